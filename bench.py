@@ -1,0 +1,373 @@
+"""Benchmark: IDW volume-mesh warping on a GB300.
+
+Headline metric: volume nodes warped per second by the mixed-precision fast
+(tree) warpMesh, on the 8M-volume-node / 150k-surface-node NACA0012 half-wing
+shell mesh with a symmetry plane (seeded synthetic inputs; twist + FFD
+surface perturbation), errTol 1e-4.  One step = setSurfaceCoordinates +
+warpMesh over the whole mesh.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` is timed with CUDA events on the library's stream with the inputs
+resident in HBM; `e2e` runs the same step through the public USMesh API with
+host arrays (surface in, warped grid out) inside the timed region.  The
+`--impl reference` arm times the CPU restatement of the reference algorithm
+(the oracle; the Fortran reference cannot be built here) on the host cores.
+"""
+import argparse
+import contextlib
+import ctypes as C
+import io
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (ni, nj, nk) of the wing shell mesh
+    "P": (577, 261, 53),   # ~8.0M volume nodes, ~150k surface nodes
+    "W": (401, 101, 50),   # ~2.0M volume nodes, ~40k surface nodes
+    "S": (101, 33, 20),    # small (tests / quick checks)
+}
+ERR_TOL = 1e-4
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def make_workload(cfg, seed=2):
+    from idwarp_gb300 import synthetic as S
+
+    ni, nj, nk = CONFIGS[cfg]
+    m = S.wing_shell(ni, nj, nk, first=1e-5, far=25.0)
+    m["xs"] = S.wing_perturbation(m["pts"], seed=seed)
+    return m
+
+
+def mesh_options(m, precision, mode="fast"):
+    return {"fileType": "NPY", "precision": precision, "evalMode": mode, "errTol": ERR_TOL,
+            "aExp": 3.0, "bExp": 5.0, "LdefFact": 1.0, "alpha": 0.25, "bucketSize": 8,
+            "symmetryPlanes": m["symmetryPlanes"]}
+
+
+def build_mesh(m, precision, mode="fast"):
+    from idwarp_gb300 import USMesh
+
+    with contextlib.redirect_stdout(io.StringIO()):
+        mesh = USMesh(options=mesh_options(m, precision, mode))
+        mesh.createCommonGrid(m["xv0"])
+        mesh.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
+    return mesh
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names[1:], parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def fp32_peak_tflops():
+    """Measured FFMA issue peak of this GPU (TFLOP/s) from a dependent-chain-free FMA probe."""
+    import torch
+
+    from idwarp_gb300 import _lib
+
+    L = _lib.load()
+    f = getattr(L, "idw_probe_ffma", None)
+    if f is None:
+        return None
+    f.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+    f.restype = C.c_int
+    stream = torch.cuda.current_stream().cuda_stream
+    out = C.c_double(0.0)
+    best = 0.0
+    for _ in range(3):
+        if f(C.c_void_p(stream), 0, C.byref(out)) == 0:
+            best = max(best, out.value)
+    return best if best > 0 else None
+
+
+def run_cpu_baseline(m, budget_s=12.0, threads=None, seed=0):
+    """Oracle (CPU restatement of the reference) warp over a seeded sample of volume nodes."""
+    from oracle.pyoracle import OracleMesh, max_threads, set_threads
+
+    if threads:
+        set_threads(threads)
+    nthr = max_threads()
+    rng = np.random.default_rng(seed)
+    nvol = len(m["xv0"])
+    # calibrate on a small sample, then size the sample to ~budget_s
+    sizes = [2000]
+    result = None
+    for attempt in range(2):
+        n = min(nvol, sizes[-1])
+        idx = np.sort(rng.choice(nvol, n, replace=False))
+        o = dict(mesh_options(m, "fp64"))
+        om = OracleMesh({k: o[k] for k in ("aExp", "bExp", "LdefFact", "alpha", "errTol", "evalMode", "bucketSize")})
+        om.set_volume(m["xv0"][idx])
+        planes = m["symmetryPlanes"]
+        om.set_symmetry(np.array([p[0] for p in planes]), np.array([p[1] for p in planes]))
+        om.set_surface_definition(m["pts"], m["conn"], m["faceSizes"])
+        om.set_surface_coordinates(m["xs"])
+        t0 = time.perf_counter()
+        om.warp()
+        dt = time.perf_counter() - t0
+        result = (n, dt)
+        if attempt == 0:
+            sizes.append(int(max(2000, min(nvol, n * budget_s / max(dt, 1e-3)))))
+    n, dt = result
+    return {"value": n / dt, "unit": "volume nodes/s", "cores": nthr, "kind": "port",
+            "sample": "%d of %d volume nodes (seeded uniform sample), fast mode errTol %g, FP64, %.2f s" % (
+                n, nvol, ERR_TOL, dt)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="P", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local_rank = _env_int("LOCAL_RANK", 0)
+    metric = "volume nodes warped/s (mixed-precision fast warpMesh)"
+    unit = "volume nodes/s"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        m = make_workload(args.config)
+        per_step = []
+        info = None
+        for s in range(args.warmup + args.steps):
+            info = run_cpu_baseline(m, budget_s=4.0, seed=100 + s)
+            if s >= args.warmup:
+                per_step.append(info["value"])
+        v = float(np.median(per_step))
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": "wing_shell_%dx%dx%d" % CONFIGS[args.config],
+                                                "errTol": ERR_TOL, "mode": "fast"},
+                "cpu_baseline": {"value": v, "unit": unit, "cores": info["cores"], "kind": "port",
+                                 "sample": info["sample"]},
+                "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "CPU restatement of the reference algorithm (oracle/idw_oracle.cpp); the Fortran/PETSc "
+                        "reference cannot be built on this image"}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist_on:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    from idwarp_gb300 import _lib
+
+    m = make_workload(args.config)
+    nvol, npts = len(m["xv0"]), len(m["pts"])
+    t_setup = time.perf_counter()
+    mesh = build_mesh(m, "mixed")
+    setup_s = time.perf_counter() - t_setup
+    L = mesh.lib
+    stream = torch.cuda.current_stream()
+    L.idw_set_stream(mesh.ctx, C.c_void_p(stream.cuda_stream))
+    xs_dev = torch.tensor(m["xs"], dtype=torch.float64, device="cuda")
+    xs_ptr = C.c_void_p(xs_dev.data_ptr())
+
+    def step():
+        L.idw_set_surface_coordinates(mesh.ctx, xs_ptr, 3 * npts, _lib.IDW_DEVICE)
+        rc = L.idw_warp_mesh(mesh.ctx)
+        if rc != 0:
+            _lib.check(L, mesh.ctx, rc, "warpMesh")
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    st = mesh.getStats()
+    kernel_ms = st["lastKernelMs"]
+    ms_step = ms_total / args.steps
+    t = torch.tensor([ms_step], device="cuda")
+    if dist_on:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_step_max = float(t.item())
+    value = world * nvol / (ms_step_max * 1e-3)
+
+    # end-to-end through the public API with host buffers
+    xs_host = np.ascontiguousarray(m["xs"])
+    for _ in range(2):
+        mesh.setSurfaceCoordinates(xs_host)
+        mesh.warpMesh()
+        grid = mesh.getWarpGrid()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        mesh.setSurfaceCoordinates(xs_host)
+        mesh.warpMesh()
+        grid = mesh.getWarpGrid()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    te = torch.tensor([e2e_s], device="cuda")
+    if dist_on:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world * nvol / float(te.item())
+
+    out = {
+        "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "wing_shell_%dx%dx%d" % CONFIGS[args.config], "volume_nodes": nvol,
+                   "surface_points": npts, "unique_surface_nodes": st["nUnique"], "errTol": ERR_TOL,
+                   "mode": "fast", "symmetry_planes": 1, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (Xv0+Xv+den0+den ~%.0f MB per step)" % (nvol * 64 / 1e6)},
+        "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": int(xs_host.nbytes),
+                "d2h_bytes_per_step": int(grid.nbytes)},
+        "clocks": clk,
+        "gpu_launches": 6 * args.steps,
+        "setup_s": setup_s,
+        "work": {"leafPairs": st["leafPairs"], "approx": st["approx"], "visited": st["visited"],
+                 "fp64Fallback": st["fp64Fallback"]},
+    }
+    # roofline of the dominant kernel (the mixed walk): FP32-issue bound
+    flops = 42.0 * (st["leafPairs"] + st["approx"])
+    peak = fp32_peak_tflops() if not args.no_extras else None
+    achieved = flops / (kernel_ms * 1e-3) / 1e12 if kernel_ms > 0 else None
+    out["roofline"] = {"bound": "fp32", "kernel": "k_walk_mixed", "achieved": achieved, "unit": "TFLOP/s",
+                       "peak": peak, "peak_source": "measured FFMA probe (idw_probe_ffma) in this run",
+                       "frac": (achieved / peak) if (achieved and peak) else None,
+                       "flops_per_launch": flops, "kernel_ms": kernel_ms, "traffic": None}
+
+    if not args.no_extras:
+        # FP64 plain GPU form on the same workload, and the precision of the mixed form against it
+        xm = grid.reshape(-1, 3).copy()
+        m64 = build_mesh(m, "fp64")
+        L.idw_set_stream(m64.ctx, C.c_void_p(stream.cuda_stream))
+        m64.setSurfaceCoordinates(xs_host)
+        m64.warpMesh()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        n64 = 2
+        for _ in range(n64):
+            L.idw_set_surface_coordinates(m64.ctx, xs_ptr, 3 * npts, _lib.IDW_DEVICE)
+            L.idw_warp_mesh(m64.ctx)
+        e1.record(stream)
+        barrier()
+        ms64 = e0.elapsed_time(e1) / n64
+        x64 = m64.getWarpGrid().reshape(-1, 3)
+        s64 = m64.getStats()
+        Ldef = st["Ldef0"]
+        errv = np.abs(xm - x64).max(axis=1) / Ldef
+        out["fp64"] = {"value": nvol / (ms64 * 1e-3), "ms_per_step": ms64,
+                       "speedup_mixed_over_fp64": ms64 / ms_step,
+                       "same_decisions": bool(s64["leafPairs"] == st["leafPairs"] and s64["approx"] == st["approx"]),
+                       "max_err_over_Ldef": float(errv.max()), "rms_err_over_Ldef": float(np.sqrt(np.mean(errv ** 2)))}
+        # 16-seed reverse derivative (FP64 adjoint) sharing one walk
+        rng = np.random.default_rng(100)
+        seeds = rng.normal(size=(16, nvol, 3))
+        sd = torch.tensor(seeds, dtype=torch.float64, device="cuda")
+        dxs = torch.zeros((16, npts, 3), dtype=torch.float64, device="cuda")
+        L.idw_warp_deriv_batch(mesh.ctx, C.c_void_p(sd.data_ptr()), 16, C.c_void_p(dxs.data_ptr()), _lib.IDW_DEVICE)
+        barrier()
+        e0.record(stream)
+        L.idw_warp_deriv_batch(mesh.ctx, C.c_void_p(sd.data_ptr()), 16, C.c_void_p(dxs.data_ptr()), _lib.IDW_DEVICE)
+        e1.record(stream)
+        barrier()
+        msd = e0.elapsed_time(e1)
+        out["warpDeriv"] = {"seeds": 16, "value": 16 * nvol / (msd * 1e-3), "unit": "seeds*nodes/s",
+                            "ms": msd, "precision": "fp64"}
+        del sd, dxs
+
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = run_cpu_baseline(m)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist_on:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,959 @@
+// C ABI of the GB300 IDW warping library (declared in include/idwarp_gb300.h).
+// One context per mesh instance owns all device state of that mesh.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/idwarp_gb300.h"
+#include "idw_host.hpp"
+#include "idw_kernels.h"
+
+using namespace idw;
+
+namespace {
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        if (p && count <= n) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+};
+
+struct Ctx {
+    int device = 0;
+    idw_options opt{};      // options now in force
+    idw_options optInit{};  // options at the last initialize (tree/error-table constants)
+    cudaStream_t stream = nullptr;
+    std::string err;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // volume
+    int64_t nVol = 0;
+    bool haveVolume = false;
+    DevBuf<double> xv0, xv, den0, den;
+    DevBuf<int> perm;
+    // symmetry
+    SymPlanes sym{};
+    // surface
+    int nPts = 0, nUnique = 0, nFaces = 0;
+    DevBuf<double> xs, xu, normals0, ptMB, tmpAi;
+    DevBuf<dbl4> ptXA;
+    DevBuf<int> xuInd, facePtr, faceConn, n2ePtr, n2e, isCorner;
+    // tree
+    int nNodes = 0, maxDepth = 0;
+    double Ldef0 = 0.0;
+    DevBuf<int4> info;
+    DevBuf<dbl4> geom;
+    DevBuf<double> nodeErr, nodeAi, nodeMB;
+    bool haveTree = false, haveWarp = false, nodalValid = false;
+    // FP32 companion arrays of the mixed-precision walk
+    DevBuf<float4> cHi, cLo, ptDA;
+    DevBuf<float> errF, ptDM, nodeDC;
+    // adjoint
+    DevBuf<double> ptAdj, nodeAdj, xub, dxs;
+    bool haveDxs = false;
+    // solver ordering
+    DevBuf<int> solverInd;
+    int64_t nSolver = -1;
+    // misc
+    DevBuf<unsigned long long> counters;
+    bool eventsRecorded = false;
+    idw_stats stats{};
+};
+
+int fail(Ctx *c, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(c, IDW_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKA(call)                                                                                         \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return fail(c, IDW_ERR_NOMEM, "allocation failed: %s", cudaGetErrorString(e_)); \
+    } while (0)
+
+int check_launch(Ctx *c, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, IDW_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+    return IDW_OK;
+}
+
+// Copy n doubles from a host or device pointer into device buffer dst.
+int copy_in(Ctx *c, double *dst, const double *src, size_t n, int where) {
+    if (n == 0) return IDW_OK;
+    if (!src) return fail(c, IDW_ERR_ARG, "null input pointer");
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), where == IDW_DEVICE ? cudaMemcpyDeviceToDevice
+                                                                           : cudaMemcpyHostToDevice,
+                       c->stream));
+    return IDW_OK;
+}
+
+int copy_out(Ctx *c, double *dst, const double *src, size_t n, int where) {
+    if (n == 0) return IDW_OK;
+    if (!dst) return fail(c, IDW_ERR_ARG, "null output pointer");
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), where == IDW_DEVICE ? cudaMemcpyDeviceToDevice
+                                                                           : cudaMemcpyDeviceToHost,
+                       c->stream));
+    if (where != IDW_DEVICE) CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+WeightLaw make_law(const Ctx *c) {
+    WeightLaw w{};
+    // exponents are fixed at tree creation (kd_tree.F90:1529-1530); Ldef and
+    // alpha^bExp are refreshed from the current options on every warp
+    // (warpMesh.F90:39-40), using the current bExp for alpha^bExp.
+    w.aExp = c->optInit.aExp;
+    w.bExp = c->optInit.bExp;
+    w.Ldef = c->Ldef0 * c->opt.LdefFact;
+    w.alphaToBexp = std::pow(c->opt.alpha, c->opt.bExp);
+    double ra = std::nearbyint(w.aExp), rb = std::nearbyint(w.bExp);
+    w.isInt = (ra == w.aExp && rb == w.bExp && ra >= 0 && rb >= ra && rb <= 64);
+    w.ia = int(ra);
+    w.ib = int(rb);
+    return w;
+}
+
+WeightLaw make_init_law(const Ctx *c) {
+    WeightLaw w = make_law(c);
+    w.Ldef = c->Ldef0 * c->optInit.LdefFact;
+    w.alphaToBexp = std::pow(c->optInit.alpha, c->optInit.bExp);
+    return w;
+}
+
+TreeDev tree_dev(Ctx *c) {
+    TreeDev t;
+    t.nNodes = c->nNodes;
+    t.info = c->info.p;
+    t.geom = c->geom.p;
+    t.err = c->nodeErr.p;
+    t.ai = c->nodeAi.p;
+    return t;
+}
+
+SurfaceDev surf_dev(Ctx *c) {
+    SurfaceDev s;
+    s.n = c->nUnique;
+    s.facePtr = c->facePtr.p;
+    s.faceConn = c->faceConn.p;
+    s.n2ePtr = c->n2ePtr.p;
+    s.n2e = c->n2e.p;
+    return s;
+}
+
+VolumeDev vol_dev(Ctx *c) {
+    VolumeDev v;
+    v.nVol = c->nVol;
+    v.perm = c->perm.p;
+    v.xv0 = c->xv0.p;
+    v.den0 = c->den0.p;
+    return v;
+}
+
+int validate_options(Ctx *c, const idw_options *o) {
+    if (!o) return fail(c, IDW_ERR_ARG, "null options");
+    if (o->evalMode != IDW_EVAL_EXACT && o->evalMode != IDW_EVAL_FAST)
+        return fail(c, IDW_ERR_ARG, "evalMode must be IDW_EVAL_EXACT or IDW_EVAL_FAST");
+    if (o->precision != IDW_PREC_FP64 && o->precision != IDW_PREC_MIXED)
+        return fail(c, IDW_ERR_ARG, "precision must be IDW_PREC_FP64 or IDW_PREC_MIXED");
+    if (o->bucketSize < 1) return fail(c, IDW_ERR_ARG, "bucketSize must be >= 1");
+    if (!(o->LdefFact > 0.0)) return fail(c, IDW_ERR_ARG, "LdefFact must be > 0");
+    return IDW_OK;
+}
+
+// Per-warp nodal properties and cluster aggregates of the current surface.
+int refresh_nodal(Ctx *c) {
+    SurfaceDev s = surf_dev(c);
+    launch_gather_xu(c->nUnique, c->xuInd.p, c->xs.p, c->xu.p, c->stream);
+    launch_nodal(s, c->xu.p, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, c->ptMB.p,
+                 c->stream);
+    launch_set_data(tree_dev(c), c->ptMB.p, c->nodeMB.p, c->stream);
+    if (c->opt.precision == IDW_PREC_MIXED) {
+        launch_mixed_nodal(c->nUnique, c->ptXA.p, c->ptMB.p, c->ptDM.p, c->stream);
+        launch_mixed_nodes(tree_dev(c), c->nodeMB.p, c->nodeDC.p, c->stream);
+    }
+    c->nodalValid = true;
+    return check_launch(c, "nodal properties");
+}
+
+bool all_finite(const double *v, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void idw_default_options(idw_options *o) {
+    std::memset(o, 0, sizeof(*o));
+    o->aExp = 3.0;
+    o->bExp = 5.0;
+    o->LdefFact = 1.0;
+    o->alpha = 0.25;
+    o->errTol = 0.0005;
+    o->symmTol = 1e-6;
+    o->cornerAngle = 30.0;
+    o->evalMode = IDW_EVAL_FAST;
+    o->useRotations = 1;
+    o->zeroCornerRotations = 1;
+    o->bucketSize = 8;
+    o->precision = IDW_PREC_MIXED;
+}
+
+int idw_create(const idw_options *opts, void **ctx_out) {
+    if (!ctx_out) return IDW_ERR_ARG;
+    *ctx_out = nullptr;
+    Ctx *c = new Ctx();
+    idw_default_options(&c->opt);
+    if (opts) {
+        int rc = validate_options(c, opts);
+        if (rc) {
+            delete c;
+            return rc;
+        }
+        c->opt = *opts;
+    }
+    c->optInit = c->opt;
+    if (cudaGetDevice(&c->device) != cudaSuccess) {
+        delete c;
+        return IDW_ERR_CUDA;
+    }
+    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        delete c;
+        return IDW_ERR_CUDA;
+    }
+    c->sym.n = 0;
+    c->sym.nLoop = 1;
+    if (c->counters.alloc(4) != cudaSuccess) {
+        delete c;
+        return IDW_ERR_NOMEM;
+    }
+    *ctx_out = c;
+    return IDW_OK;
+}
+
+int idw_destroy(void *ctx) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    delete c;
+    return IDW_OK;
+}
+
+int idw_last_error(void *ctx, char *buf, int len) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c || !buf || len <= 0) return IDW_ERR_ARG;
+    std::snprintf(buf, size_t(len), "%s", c->err.c_str());
+    return IDW_OK;
+}
+
+int idw_set_stream(void *ctx, void *stream) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    c->stream = static_cast<cudaStream_t>(stream);
+    return IDW_OK;
+}
+
+int idw_synchronize(void *ctx) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_set_options(void *ctx, const idw_options *opts) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    int rc = validate_options(c, opts);
+    if (rc) return rc;
+    if (opts->useRotations != c->opt.useRotations || opts->precision != c->opt.precision) c->nodalValid = false;
+    c->opt = *opts;
+    return IDW_OK;
+}
+
+int idw_create_common_grid(void *ctx, const double *volnodes, int64_t nvol, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (nvol < 0 || nvol > (int64_t(1) << 31) - 1) return fail(c, IDW_ERR_ARG, "nvol out of range: %lld", (long long)nvol);
+    CK(cudaSetDevice(c->device));
+    c->nVol = nvol;
+    CKA(c->xv0.alloc(3 * nvol));
+    CKA(c->xv.alloc(3 * nvol));
+    CKA(c->den0.alloc(nvol));
+    CKA(c->den.alloc(nvol));
+    CKA(c->perm.alloc(nvol));
+    int rc = copy_in(c, c->xv0.p, volnodes, 3 * size_t(nvol), where);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->xv.p, c->xv0.p, 3 * nvol * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    // bounding box on the host (set-up only)
+    std::vector<double> h(3 * size_t(nvol));
+    CK(cudaMemcpyAsync(h.data(), c->xv0.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!all_finite(h.data(), h.size())) return fail(c, IDW_ERR_NONFINITE, "non-finite volume coordinates");
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (nvol > 0) {
+        for (int k = 0; k < 3; ++k) lo[k] = hi[k] = h[k];
+        for (int64_t i = 0; i < nvol; ++i)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = std::min(lo[k], h[3 * i + k]);
+                hi[k] = std::max(hi[k], h[3 * i + k]);
+            }
+        DevBuf<unsigned long long> codes, codesAlt;
+        DevBuf<int> idx;
+        CKA(codes.alloc(nvol));
+        CKA(codesAlt.alloc(nvol));
+        CKA(idx.alloc(nvol));
+        launch_morton_codes(nvol, c->xv0.p, lo, hi, codes.p, idx.p, c->stream);
+        if (sort_morton(nvol, codes.p, idx.p, codesAlt.p, c->perm.p, c->stream))
+            return fail(c, IDW_ERR_NOMEM, "Morton sort failed");
+        int e = check_launch(c, "morton");
+        if (e) return e;
+    }
+    c->haveVolume = true;
+    c->haveWarp = false;
+    c->haveDxs = false;
+    c->stats.nVol = nvol;
+    return IDW_OK;
+}
+
+int idw_set_symmetry_planes(void *ctx, const double *pts, const double *normals, int32_t n) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (n < 0 || n > kMaxSym) return fail(c, IDW_ERR_LIMIT, "at most %d symmetry planes are supported", kMaxSym);
+    if (n > 0 && (!pts || !normals)) return fail(c, IDW_ERR_ARG, "null symmetry arrays");
+    c->sym.n = n;
+    c->sym.nLoop = 1 << n;
+    for (int j = 0; j < n; ++j)
+        for (int k = 0; k < 3; ++k) {
+            c->sym.p[j][k] = pts[3 * j + k];
+            c->sym.nrm[j][k] = normals[3 * j + k];
+        }
+    c->stats.nLoop = c->sym.nLoop;
+    return IDW_OK;
+}
+
+int idw_point_reduce(const double *pts, int32_t n, double tol, double *uniquepts, int32_t *link, int32_t *nunique) {
+    if (n < 0 || !nunique || (n > 0 && (!pts || !uniquepts || !link))) return IDW_ERR_ARG;
+    *nunique = point_reduce(pts, n, tol, uniquepts, link);
+    return IDW_OK;
+}
+
+int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const double *uniquepts, int32_t nunique,
+                           const int32_t *link, const int32_t *faceSizes, int32_t nfaces, const int32_t *faceConn,
+                           int32_t nconn) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    if (!c->haveVolume) return fail(c, IDW_ERR_STATE, "the volume grid must be set before the surface definition");
+    if (nunique < 1 || npts < 1) return fail(c, IDW_ERR_ARG, "empty surface (npts=%d, nunique=%d)", npts, nunique);
+    if (!pts || !uniquepts || !link || !faceSizes || !faceConn) return fail(c, IDW_ERR_ARG, "null surface array");
+    if (!all_finite(pts, 3 * size_t(npts)) || !all_finite(uniquepts, 3 * size_t(nunique)))
+        return fail(c, IDW_ERR_NONFINITE, "non-finite surface coordinates");
+    std::vector<int> fptr(nfaces + 1, 0);
+    for (int f = 0; f < nfaces; ++f) {
+        if (faceSizes[f] < 1 || faceSizes[f] > kMaxFacePts)
+            return fail(c, IDW_ERR_LIMIT, "face %d has %d points (supported: 1..%d)", f, faceSizes[f], kMaxFacePts);
+        fptr[f + 1] = fptr[f] + faceSizes[f];
+    }
+    if (fptr[nfaces] != nconn) return fail(c, IDW_ERR_ARG, "sum(faceSizes)=%d != len(conn)=%d", fptr[nfaces], nconn);
+    for (int i = 0; i < npts; ++i)
+        if (link[i] < 1 || link[i] > nunique) return fail(c, IDW_ERR_ARG, "link[%d]=%d out of range", i, link[i]);
+    for (int i = 0; i < nconn; ++i)
+        if (faceConn[i] < 0 || faceConn[i] >= npts) return fail(c, IDW_ERR_ARG, "conn[%d]=%d out of range", i, faceConn[i]);
+    c->optInit = c->opt;
+    c->haveTree = c->haveWarp = c->haveDxs = c->nodalValid = false;
+
+    FlatTree t;
+    build_kdtree(uniquepts, nunique, c->opt.bucketSize, t);
+    const int n = nunique, nn = t.nodes();
+    std::vector<int> inv(n);
+    for (int i = 0; i < n; ++i) inv[t.perm[i]] = i;
+    std::vector<dbl4> xa(n);
+    for (int i = 0; i < n; ++i) {
+        const double *q = uniquepts + 3 * t.perm[i];
+        xa[i] = mk_dbl4(q[0], q[1], q[2], 0.0);
+    }
+    std::vector<int> tconn(nconn);
+    for (int i = 0; i < nconn; ++i) tconn[i] = inv[link[faceConn[i]] - 1];
+    std::vector<int> cnt(n + 1, 0);
+    for (int i = 0; i < nconn; ++i) cnt[tconn[i] + 1]++;
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> n2e(nconn), fill(cnt.begin(), cnt.end() - 1);
+    for (int f = 0; f < nfaces; ++f)
+        for (int j = fptr[f]; j < fptr[f + 1]; ++j) n2e[fill[tconn[j]]++] = f;
+    std::vector<int> xuInd(n, -1);
+    for (int i = 0; i < npts; ++i) {
+        int q = inv[link[i] - 1];
+        if (xuInd[q] < 0) xuInd[q] = i;
+    }
+    // Ldef0: largest distance from the centroid (kd_tree.F90:1500-1512)
+    double cen[3] = {0, 0, 0};
+    for (int i = 0; i < n; ++i) {
+        cen[0] += xa[i].x;
+        cen[1] += xa[i].y;
+        cen[2] += xa[i].z;
+    }
+    for (int k = 0; k < 3; ++k) cen[k] = cen[k] / n;
+    double L0 = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double *q = uniquepts + 3 * i;
+        double dx = q[0] - cen[0], dy = q[1] - cen[1], dz = q[2] - cen[2];
+        L0 = std::max(L0, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    c->Ldef0 = L0;
+    c->nPts = npts;
+    c->nUnique = n;
+    c->nFaces = nfaces;
+    c->nNodes = nn;
+    c->maxDepth = t.maxDepth;
+    // device arrays
+    CKA(c->xs.alloc(3 * size_t(npts)));
+    CKA(c->dxs.alloc(3 * size_t(npts)));
+    CKA(c->xu.alloc(3 * size_t(n)));
+    CKA(c->xub.alloc(3 * size_t(n)));
+    CKA(c->normals0.alloc(3 * size_t(n)));
+    CKA(c->tmpAi.alloc(n));
+    CKA(c->ptMB.alloc(12 * size_t(n)));
+    CKA(c->ptAdj.alloc(12 * size_t(n)));
+    CKA(c->ptXA.alloc(n));
+    CKA(c->xuInd.alloc(n));
+    CKA(c->isCorner.alloc(n));
+    CKA(c->facePtr.alloc(nfaces + 1));
+    CKA(c->faceConn.alloc(std::max(nconn, 1)));
+    CKA(c->n2ePtr.alloc(n + 1));
+    CKA(c->n2e.alloc(std::max(nconn, 1)));
+    CKA(c->info.alloc(nn));
+    CKA(c->geom.alloc(nn));
+    CKA(c->nodeErr.alloc(kNerr * size_t(nn)));
+    CKA(c->nodeAi.alloc(nn));
+    CKA(c->nodeMB.alloc(12 * size_t(nn)));
+    CKA(c->nodeAdj.alloc(12 * size_t(nn)));
+    CKA(c->cHi.alloc(nn));
+    CKA(c->cLo.alloc(nn));
+    CKA(c->errF.alloc(kNerr * size_t(nn)));
+    CKA(c->nodeDC.alloc(12 * size_t(nn)));
+    CKA(c->ptDA.alloc(n));
+    CKA(c->ptDM.alloc(12 * size_t(n)));
+    cudaStream_t st = c->stream;
+    CK(cudaMemcpyAsync(c->xs.p, pts, 3 * sizeof(double) * npts, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->xuInd.p, xuInd.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->facePtr.p, fptr.data(), sizeof(int) * (nfaces + 1), cudaMemcpyHostToDevice, st));
+    if (nconn > 0) {
+        CK(cudaMemcpyAsync(c->faceConn.p, tconn.data(), sizeof(int) * nconn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->n2e.p, n2e.data(), sizeof(int) * nconn, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(c->n2ePtr.p, cnt.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st));
+    std::vector<int4> info(nn);
+    std::vector<dbl4> geom(nn);
+    for (int k = 0; k < nn; ++k) {
+        info[k] = make_int4(t.l[k], t.u[k], t.escape[k], t.leaf[k]);
+        geom[k] = mk_dbl4(t.X[3 * k], t.X[3 * k + 1], t.X[3 * k + 2], t.oradius[k]);
+    }
+    CK(cudaMemcpyAsync(c->info.p, info.data(), sizeof(int4) * nn, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->geom.p, geom.data(), sizeof(dbl4) * nn, cudaMemcpyHostToDevice, st));
+    // initial nodal properties: normals0, Ai, corners (kd_tree.F90:1547-1578)
+    SurfaceDev s = surf_dev(c);
+    launch_gather_xu(n, c->xuInd.p, c->xs.p, c->xu.p, st);
+    launch_nodal_init(s, c->xu.p, c->normals0.p, c->tmpAi.p, st);
+    double thr = std::cos(c->opt.cornerAngle * 3.1415926535897931 / 180.0);
+    launch_corners(s, c->xu.p, c->normals0.p, thr, c->opt.zeroCornerRotations, c->isCorner.p, st);
+    int e = check_launch(c, "nodal init");
+    if (e) return e;
+    std::vector<double> ai(n), nodeAi(nn, 0.0);
+    CK(cudaMemcpyAsync(ai.data(), c->tmpAi.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // setAi: leaf sums in range order, interior = left + right (kd_tree.F90:536-556)
+    for (int k = nn - 1; k >= 0; --k) {
+        if (t.leaf[k]) {
+            double a = 0.0;
+            for (int i = t.l[k]; i <= t.u[k]; ++i) a = a + ai[i];
+            nodeAi[k] = a;
+        } else {
+            nodeAi[k] = nodeAi[k + 1] + nodeAi[t.escape[k + 1]];
+        }
+    }
+    for (int i = 0; i < n; ++i) xa[i].w = ai[i];
+    CK(cudaMemcpyAsync(c->ptXA.p, xa.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->nodeAi.p, nodeAi.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
+    // error tables (kd_tree.F90:1528-1544) with the creation-time law
+    WeightLaw law0 = make_init_law(c);
+    launch_compute_errors(tree_dev(c), c->ptXA.p, law0, c->nodeErr.p, nullptr, 0, st);
+    e = check_launch(c, "computeErrors");
+    if (e) return e;
+    // FP32 companions: split centroids, radii, areas, error tables, leaf offsets
+    {
+        std::vector<float4> hi(nn), lo(nn), da(n);
+        for (int k = 0; k < nn; ++k) {
+            float h[3], l[3];
+            for (int q = 0; q < 3; ++q) {
+                h[q] = float(t.X[3 * k + q]);
+                l[q] = float(t.X[3 * k + q] - double(h[q]));
+            }
+            hi[k] = make_float4(h[0], h[1], h[2], float(t.oradius[k]));
+            lo[k] = make_float4(l[0], l[1], l[2], float(nodeAi[k]));
+            if (t.leaf[k]) {
+                for (int i = t.l[k]; i <= t.u[k]; ++i)
+                    da[i] = make_float4(float(xa[i].x - t.X[3 * k]), float(xa[i].y - t.X[3 * k + 1]),
+                                        float(xa[i].z - t.X[3 * k + 2]), float(ai[i]));
+            }
+        }
+        CK(cudaMemcpyAsync(c->cHi.p, hi.data(), sizeof(float4) * nn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->cLo.p, lo.data(), sizeof(float4) * nn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->ptDA.p, da.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
+        launch_to_float(int64_t(kNerr) * nn, c->nodeErr.p, c->errF.p, st);
+        CK(cudaStreamSynchronize(st));
+    }
+    // denominator estimate over the mirrors (initializeWarping.F90:241-247)
+    launch_denominator0(tree_dev(c), c->ptXA.p, vol_dev(c), law0, c->sym, c->den0.p, st);
+    e = check_launch(c, "denominator0");
+    if (e) return e;
+    CK(cudaStreamSynchronize(st));
+    c->haveTree = true;
+    c->stats.nUnique = n;
+    c->stats.nTreeNodes = nn;
+    c->stats.maxDepth = t.maxDepth;
+    c->stats.nSurfPts = npts;
+    c->stats.nLoop = c->sym.nLoop;
+    c->stats.Ldef0 = L0;
+    return IDW_OK;
+}
+
+int idw_set_surface_coordinates(void *ctx, const double *coords, int64_t cdof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (cdof != 3 * int64_t(c->nPts))
+        return fail(c, IDW_ERR_ARG, "incorrect length of coordinates: expected %lld, received %lld",
+                    (long long)(3 * int64_t(c->nPts)), (long long)cdof);
+    CK(cudaSetDevice(c->device));
+    if (where != IDW_DEVICE && !all_finite(coords, size_t(cdof)))
+        return fail(c, IDW_ERR_NONFINITE, "non-finite surface coordinates");
+    int rc = copy_in(c, c->xs.p, coords, size_t(cdof), where);
+    if (rc) return rc;
+    if (where != IDW_DEVICE) CK(cudaStreamSynchronize(c->stream));
+    c->nodalValid = false;
+    return IDW_OK;
+}
+
+int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (cdof != 3 * int64_t(c->nPts)) return fail(c, IDW_ERR_ARG, "cdof mismatch");
+    CK(cudaSetDevice(c->device));
+    return copy_out(c, coords, c->xs.p, size_t(cdof), where);
+}
+
+static int run_warp(Ctx *c, double *xvOut, double *denOut) {
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    int rc = refresh_nodal(c);
+    if (rc) return rc;
+    EvalConsts k;
+    k.law = make_law(c);
+    k.errTol = c->opt.errTol;
+    k.sym = c->sym;
+    PointsDev p;
+    p.xa = c->ptXA.p;
+    p.mb = c->ptMB.p;
+    WalkOut o;
+    o.xv = xvOut;
+    o.den = denOut;
+    o.counters = c->counters.p;
+    CK(cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+    CK(cudaEventRecord(c->ev0, c->stream));
+    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
+    if (c->opt.precision == IDW_PREC_MIXED) {
+        TreeDevF tf;
+        tf.cHi = c->cHi.p;
+        tf.cLo = c->cLo.p;
+        tf.err = c->errF.p;
+        PointsDevF pf;
+        pf.da = c->ptDA.p;
+        pf.dm = c->ptDM.p;
+        NodeAggF af;
+        af.dc = c->nodeDC.p;
+        launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), k, exact, o, c->stream);
+    } else {
+        launch_walk_fp64(tree_dev(c), p, vol_dev(c), c->nodeMB.p, k, exact, c->nUnique, o, c->stream);
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    c->eventsRecorded = true;
+    return check_launch(c, "warp");
+}
+
+static int read_counters(Ctx *c) {
+    unsigned long long h[4];
+    CK(cudaMemcpyAsync(h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->stats.leafPairs = int64_t(h[0]);
+    c->stats.approx = int64_t(h[1]);
+    c->stats.visited = int64_t(h[2]);
+    c->stats.fp64Fallback = int64_t(h[3]);
+    if (c->eventsRecorded) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->stats.lastKernelMs = ms;
+        (void)cudaGetLastError();
+    }
+    return IDW_OK;
+}
+
+int idw_warp_mesh(void *ctx) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    int rc = run_warp(c, c->xv.p, c->den.p);
+    if (rc) return rc;
+    c->haveWarp = true;
+    return IDW_OK;
+}
+
+int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double *out, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (nbatch < 0 || !coords || !out) return fail(c, IDW_ERR_ARG, "bad batch arguments");
+    CK(cudaSetDevice(c->device));
+    const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
+    // keep the context's own surface: stage it and restore afterwards
+    DevBuf<double> keep, tmpOut;
+    CKA(keep.alloc(sdof));
+    CK(cudaMemcpyAsync(keep.p, c->xs.p, sdof * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    if (where != IDW_DEVICE) CKA(tmpOut.alloc(vdof));
+    for (int b = 0; b < nbatch; ++b) {
+        int rc = copy_in(c, c->xs.p, coords + b * sdof, sdof, where);
+        if (rc) return rc;
+        double *dst = (where == IDW_DEVICE) ? out + b * vdof : tmpOut.p;
+        rc = run_warp(c, dst, nullptr);
+        if (rc) return rc;
+        if (where != IDW_DEVICE) {
+            rc = copy_out(c, out + b * vdof, tmpOut.p, vdof, IDW_HOST);
+            if (rc) return rc;
+        }
+    }
+    CK(cudaMemcpyAsync(c->xs.p, keep.p, sdof * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->nodalValid = false;
+    return IDW_OK;
+}
+
+int idw_get_volume_coordinates(void *ctx, double *out, int64_t ndof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof != 3 * c->nVol) return fail(c, IDW_ERR_ARG, "ndof mismatch: %lld vs %lld", (long long)ndof, (long long)(3 * c->nVol));
+    CK(cudaSetDevice(c->device));
+    return copy_out(c, out, c->xv.p, size_t(ndof), where);
+}
+
+int idw_get_common_volume_coordinates(void *ctx, double *out, int64_t ndof, int where) {
+    return idw_get_volume_coordinates(ctx, out, ndof, where);
+}
+
+int idw_set_volume_coordinates(void *ctx, const double *in, int64_t ndof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof != 3 * c->nVol) return fail(c, IDW_ERR_ARG, "ndof mismatch");
+    CK(cudaSetDevice(c->device));
+    int rc = copy_in(c, c->xv.p, in, size_t(ndof), where);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_get_stats(void *ctx, idw_stats *out) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c || !out) return IDW_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    int rc = read_counters(c);
+    if (rc) return rc;
+    *out = c->stats;
+    return IDW_OK;
+}
+
+int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (nvol != c->nVol) return fail(c, IDW_ERR_ARG, "nvol mismatch");
+    CK(cudaSetDevice(c->device));
+    return copy_out(c, out, c->den0.p, size_t(nvol), where);
+}
+
+static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStride, double *dxsOut, int where,
+                     int64_t dxsStride) {
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDeriv");
+    int rc = refresh_nodal(c);
+    if (rc) return rc;
+    EvalConsts k;
+    k.law = make_law(c);
+    k.errTol = c->opt.errTol;
+    k.sym = c->sym;
+    PointsDev p;
+    p.xa = c->ptXA.p;
+    p.mb = c->ptMB.p;
+    const int n = c->nUnique, nn = c->nNodes;
+    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
+    DevBuf<double> ptAdj, nodeAdj;
+    CKA(ptAdj.alloc(size_t(nSeeds) * 12 * n));
+    CKA(nodeAdj.alloc(size_t(nSeeds) * 12 * nn));
+    CK(cudaMemsetAsync(ptAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * n, c->stream));
+    CK(cudaMemsetAsync(nodeAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * nn, c->stream));
+    CK(cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+    CK(cudaEventRecord(c->ev0, c->stream));
+    launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride, ptAdj.p,
+                             nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
+    CK(cudaEventRecord(c->ev1, c->stream));
+    c->eventsRecorded = true;
+    rc = check_launch(c, "adjoint walk");
+    if (rc) return rc;
+    SurfaceDev s = surf_dev(c);
+    for (int sd = 0; sd < nSeeds; ++sd) {
+        double *pa = ptAdj.p + size_t(sd) * 12 * n;
+        launch_set_data_b(tree_dev(c), nodeAdj.p + size_t(sd) * 12 * nn, pa, n, c->stream);
+        CK(cudaMemsetAsync(c->xub.p, 0, sizeof(double) * 3 * n, c->stream));
+        launch_nodal_b(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa, c->xub.p,
+                       c->stream);
+        double *dst = (where == IDW_DEVICE) ? dxsOut + sd * dxsStride : c->dxs.p;
+        CK(cudaMemsetAsync(dst, 0, sizeof(double) * 3 * c->nPts, c->stream));
+        launch_scatter_dxs(n, c->xuInd.p, c->xub.p, dst, c->stream);
+        rc = check_launch(c, "reverse nodal properties");
+        if (rc) return rc;
+        if (where != IDW_DEVICE && dxsOut) {
+            rc = copy_out(c, dxsOut + sd * dxsStride, c->dxs.p, 3 * size_t(c->nPts), IDW_HOST);
+            if (rc) return rc;
+        }
+    }
+    return IDW_OK;
+}
+
+int idw_warp_deriv(void *ctx, const double *dxv, int64_t ndof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof != 3 * c->nVol) return fail(c, IDW_ERR_ARG, "dXv has %lld entries, expected %lld", (long long)ndof, (long long)(3 * c->nVol));
+    CK(cudaSetDevice(c->device));
+    const double *d = dxv;
+    DevBuf<double> tmp;
+    if (where != IDW_DEVICE) {
+        CKA(tmp.alloc(size_t(ndof)));
+        int rc = copy_in(c, tmp.p, dxv, size_t(ndof), IDW_HOST);
+        if (rc) return rc;
+        d = tmp.p;
+    }
+    int rc = run_deriv(c, d, 1, ndof, c->dxs.p, IDW_DEVICE, 3 * int64_t(c->nPts));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    c->haveDxs = true;
+    return IDW_OK;
+}
+
+int idw_get_dxs(void *ctx, double *out, int64_t ndof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof != 3 * int64_t(c->nPts)) return fail(c, IDW_ERR_ARG, "ndof mismatch");
+    if (!c->haveDxs) return fail(c, IDW_ERR_STATE, "warpDeriv has not been called");
+    CK(cudaSetDevice(c->device));
+    return copy_out(c, out, c->dxs.p, size_t(ndof), where);
+}
+
+int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *dxs, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (nseeds < 1 || !dxv || !dxs) return fail(c, IDW_ERR_ARG, "bad seed arguments");
+    CK(cudaSetDevice(c->device));
+    const size_t vdof = 3 * size_t(c->nVol);
+    const double *d = dxv;
+    DevBuf<double> tmp;
+    if (where != IDW_DEVICE) {
+        CKA(tmp.alloc(vdof * nseeds));
+        int rc = copy_in(c, tmp.p, dxv, vdof * nseeds, IDW_HOST);
+        if (rc) return rc;
+        d = tmp.p;
+    }
+    int rc = run_deriv(c, d, nseeds, int64_t(vdof), dxs, where, 3 * int64_t(c->nPts));
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_set_external_mesh_indices(void *ctx, const int32_t *ind, int64_t ndof_solver) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof_solver < 0 || (ndof_solver > 0 && !ind)) return fail(c, IDW_ERR_ARG, "bad solver indices");
+    for (int64_t k = 0; k < ndof_solver; ++k)
+        if (ind[k] < 0 || ind[k] >= 3 * c->nVol)
+            return fail(c, IDW_ERR_ARG, "solver index %d out of range", ind[k]);
+    CK(cudaSetDevice(c->device));
+    CKA(c->solverInd.alloc(std::max<int64_t>(ndof_solver, 1)));
+    if (ndof_solver > 0)
+        CK(cudaMemcpyAsync(c->solverInd.p, ind, sizeof(int) * ndof_solver, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->nSolver = ndof_solver;
+    return IDW_OK;
+}
+
+int idw_get_solver_mesh_dof(void *ctx, int64_t *ndof) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c || !ndof) return IDW_ERR_ARG;
+    *ndof = c->nSolver;
+    return IDW_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void k_gather_dof(int64_t n, const int *ind, const double *src, double *dst) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = src[ind[k]];
+}
+__global__ void k_scatter_add_dof(int64_t n, const int *ind, const double *src, double *dst) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) atomicAdd(dst + ind[k], src[k]);
+}
+}  // namespace
+
+extern "C" {
+
+int idw_warp_to_solver_grid(void *ctx, const double *warp, int64_t wdof, double *solver, int64_t sdof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (c->nSolver < 0) return fail(c, IDW_ERR_STATE, "setExternalMeshIndices has not been called");
+    if (wdof != 3 * c->nVol || sdof != c->nSolver) return fail(c, IDW_ERR_ARG, "size mismatch");
+    CK(cudaSetDevice(c->device));
+    DevBuf<double> w, s;
+    const double *wp = warp;
+    double *sp = solver;
+    if (where != IDW_DEVICE) {
+        CKA(w.alloc(size_t(wdof)));
+        CKA(s.alloc(size_t(sdof)));
+        int rc = copy_in(c, w.p, warp, size_t(wdof), IDW_HOST);
+        if (rc) return rc;
+        wp = w.p;
+        sp = s.p;
+    }
+    if (sdof > 0) k_gather_dof<<<int((sdof + 255) / 256), 256, 0, c->stream>>>(sdof, c->solverInd.p, wp, sp);
+    int rc = check_launch(c, "warp_to_solver");
+    if (rc) return rc;
+    if (where != IDW_DEVICE) return copy_out(c, solver, s.p, size_t(sdof), IDW_HOST);
+    return IDW_OK;
+}
+
+int idw_solver_to_warp_grid(void *ctx, const double *solver, int64_t sdof, double *warp, int64_t wdof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (c->nSolver < 0) return fail(c, IDW_ERR_STATE, "setExternalMeshIndices has not been called");
+    if (wdof != 3 * c->nVol || sdof != c->nSolver) return fail(c, IDW_ERR_ARG, "size mismatch");
+    CK(cudaSetDevice(c->device));
+    DevBuf<double> w, s;
+    const double *sp = solver;
+    double *wp = warp;
+    if (where != IDW_DEVICE) {
+        CKA(w.alloc(size_t(wdof)));
+        CKA(s.alloc(size_t(sdof)));
+        int rc = copy_in(c, s.p, solver, size_t(sdof), IDW_HOST);
+        if (rc) return rc;
+        sp = s.p;
+        wp = w.p;
+    }
+    CK(cudaMemsetAsync(wp, 0, sizeof(double) * wdof, c->stream));
+    if (sdof > 0) k_scatter_add_dof<<<int((sdof + 255) / 256), 256, 0, c->stream>>>(sdof, c->solverInd.p, sp, wp);
+    int rc = check_launch(c, "solver_to_warp");
+    if (rc) return rc;
+    if (where != IDW_DEVICE) return copy_out(c, warp, w.p, size_t(wdof), IDW_HOST);
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_get_tree(void *ctx, int32_t *nodeInfo, double *nodeGeom, double *nodeErr, double *nodeAi) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    CK(cudaSetDevice(c->device));
+    const int nn = c->nNodes;
+    if (nodeInfo) CK(cudaMemcpyAsync(nodeInfo, c->info.p, sizeof(int4) * nn, cudaMemcpyDeviceToHost, c->stream));
+    if (nodeGeom) CK(cudaMemcpyAsync(nodeGeom, c->geom.p, sizeof(dbl4) * nn, cudaMemcpyDeviceToHost, c->stream));
+    if (nodeErr) CK(cudaMemcpyAsync(nodeErr, c->nodeErr.p, sizeof(double) * kNerr * nn, cudaMemcpyDeviceToHost, c->stream));
+    if (nodeAi) CK(cudaMemcpyAsync(nodeAi, c->nodeAi.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_get_surface_state(void *ctx, double *xu0, double *ai, double *normals0, int32_t *isCorner, int32_t *xuInd) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    CK(cudaSetDevice(c->device));
+    const int n = c->nUnique;
+    std::vector<dbl4> xa(n);
+    CK(cudaMemcpyAsync(xa.data(), c->ptXA.p, sizeof(dbl4) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (normals0) CK(cudaMemcpyAsync(normals0, c->normals0.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    if (isCorner) CK(cudaMemcpyAsync(isCorner, c->isCorner.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (xuInd) CK(cudaMemcpyAsync(xuInd, c->xuInd.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; ++i) {
+        if (xu0) {
+            xu0[3 * i] = xa[i].x;
+            xu0[3 * i + 1] = xa[i].y;
+            xu0[3 * i + 2] = xa[i].z;
+        }
+        if (ai) ai[i] = xa[i].w;
+    }
+    return IDW_OK;
+}
+
+int idw_get_nodal_properties(void *ctx, double *mi, double *bi) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    CK(cudaSetDevice(c->device));
+    if (!c->nodalValid) {
+        int rc = refresh_nodal(c);
+        if (rc) return rc;
+    }
+    const int n = c->nUnique;
+    std::vector<double> mb(12 * size_t(n));
+    CK(cudaMemcpyAsync(mb.data(), c->ptMB.p, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; ++i) {
+        if (mi) std::memcpy(mi + 9 * i, &mb[12 * i], 9 * sizeof(double));
+        if (bi) std::memcpy(bi + 3 * i, &mb[12 * i + 9], 3 * sizeof(double));
+    }
+    return IDW_OK;
+}
+
+}  // extern "C"

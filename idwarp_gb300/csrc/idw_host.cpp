@@ -1,0 +1,173 @@
+#include "idw_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+
+namespace idw {
+
+namespace {
+
+struct CellKey {
+    int64_t x, y, z;
+    bool operator==(const CellKey &o) const { return x == o.x && y == o.y && z == o.z; }
+};
+struct CellHash {
+    size_t operator()(const CellKey &k) const {
+        uint64_t h = uint64_t(k.x) * 0x9E3779B97F4A7C15ull;
+        h ^= uint64_t(k.y) * 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
+        h ^= uint64_t(k.z) * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
+        return size_t(h);
+    }
+};
+
+}  // namespace
+
+int point_reduce(const double *pts, int n, double tol, double *uniquePts, int32_t *link) {
+    if (n <= 0) return 0;
+    // Uniform hash grid with cells no smaller than tol, so every partner of a
+    // point lies in the 27 cells around it.
+    double lo[3] = {pts[0], pts[1], pts[2]}, hi[3] = {pts[0], pts[1], pts[2]};
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], pts[3 * i + k]);
+            hi[k] = std::max(hi[k], pts[3 * i + k]);
+        }
+    double ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-300});
+    double h = std::max(tol, ext * std::ldexp(1.0, -40));
+    std::unordered_map<CellKey, std::vector<int32_t>, CellHash> grid;
+    grid.reserve(size_t(n) * 2);
+    auto cell = [&](const double *p) {
+        return CellKey{int64_t(std::floor((p[0] - lo[0]) / h)), int64_t(std::floor((p[1] - lo[1]) / h)),
+                       int64_t(std::floor((p[2] - lo[2]) / h))};
+    };
+    for (int i = 0; i < n; ++i) grid[cell(pts + 3 * i)].push_back(i);
+    const double tol2 = tol * tol;
+    std::memset(link, 0, sizeof(int32_t) * n);
+    int nUnique = 0;
+    for (int i = 0; i < n; ++i) {
+        if (link[i] != 0) continue;
+        const double *p = pts + 3 * i;
+        ++nUnique;
+        std::memcpy(uniquePts + 3 * (nUnique - 1), p, 3 * sizeof(double));
+        CellKey c = cell(p);
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dz = -1; dz <= 1; ++dz) {
+                    auto it = grid.find(CellKey{c.x + dx, c.y + dy, c.z + dz});
+                    if (it == grid.end()) continue;
+                    for (int32_t j : it->second) {
+                        const double *q = pts + 3 * j;
+                        double ax = q[0] - p[0], ay = q[1] - p[1], az = q[2] - p[2];
+                        if (ax * ax + ay * ay + az * az <= tol2) link[j] = nUnique;
+                    }
+                }
+    }
+    return nUnique;
+}
+
+namespace {
+
+// Spread of axis c over ranks [l,u] of perm, sampling ranks l..min(u,l+200)
+// pairwise as the reference does (kd_tree.F90:257-298).
+double sampled_spread(const double *p, const int32_t *perm, int c, int l, int u) {
+    double smin = p[3 * perm[l] + c], smax = smin;
+    int last = std::min(u, l + 200);
+    int i = l + 2;
+    for (; i <= last; i += 2) {
+        double a = p[3 * perm[i - 1] + c], b = p[3 * perm[i] + c];
+        if (a > b) std::swap(a, b);
+        smin = std::min(smin, a);
+        smax = std::max(smax, b);
+    }
+    if (i == last + 1) {
+        double z = p[3 * perm[last] + c];
+        smin = std::min(smin, z);
+        smax = std::max(smax, z);
+    }
+    return smax - smin;
+}
+
+// Partial selection of rank k in [lo, hi] on axis c with the first element of
+// the current window as pivot (kd_tree.F90:199-231).
+void select_rank(const double *p, int32_t *perm, int c, int k, int lo, int hi) {
+    while (lo < hi) {
+        const double pivot = p[3 * perm[lo] + c];
+        int m = lo;
+        for (int i = lo + 1; i <= hi; ++i)
+            if (p[3 * perm[i] + c] < pivot) std::swap(perm[++m], perm[i]);
+        std::swap(perm[lo], perm[m]);
+        if (m <= k) lo = m + 1;
+        if (m >= k) hi = m - 1;
+    }
+}
+
+}  // namespace
+
+void build_kdtree(const double *pts, int n, int bucket, FlatTree &t) {
+    t = FlatTree();
+    t.n = n;
+    t.bucket = bucket;
+    t.perm.resize(n);
+    for (int i = 0; i < n; ++i) t.perm[i] = i;
+    struct Item {
+        int l, u, depth, parentSlot;
+    };
+    // Preorder: pop a range, give it the next id, push right then left.
+    std::vector<Item> work;
+    work.push_back({0, n - 1, 1, -1});
+    std::vector<int32_t> rightChild;
+    while (!work.empty()) {
+        Item it = work.back();
+        work.pop_back();
+        int id = int(t.l.size());
+        t.l.push_back(it.l);
+        t.u.push_back(it.u);
+        t.depth.push_back(it.depth);
+        t.escape.push_back(-1);
+        rightChild.push_back(-1);
+        t.maxDepth = std::max(t.maxDepth, it.depth);
+        if (it.parentSlot >= 0) rightChild[it.parentSlot] = id;
+        if (it.u - it.l <= bucket) {
+            t.leaf.push_back(1);
+            continue;
+        }
+        t.leaf.push_back(0);
+        int best = 0;
+        double bsp = -1.0;
+        for (int c = 0; c < 3; ++c) {
+            double sp = sampled_spread(pts, t.perm.data(), c, it.l, it.u);
+            if (sp > bsp) {
+                best = c;
+                bsp = sp;
+            }
+        }
+        int m = (it.l + it.u) / 2;
+        select_rank(pts, t.perm.data(), best, m, it.l, it.u);
+        work.push_back({m + 1, it.u, it.depth + 1, id});  // right: id recorded when popped
+        work.push_back({it.l, m, it.depth + 1, -1});      // left child gets id+1
+    }
+    const int nn = t.nodes();
+    for (int k = nn - 1; k >= 0; --k) t.escape[k] = t.leaf[k] ? k + 1 : t.escape[rightChild[k]];
+    // setCenters: unweighted centroid of the range, 1/max distance
+    t.X.assign(3 * nn, 0.0);
+    t.oradius.assign(nn, 0.0);
+    for (int k = 0; k < nn; ++k) {
+        double s[3] = {0, 0, 0};
+        for (int i = t.l[k]; i <= t.u[k]; ++i)
+            for (int c = 0; c < 3; ++c) s[c] += pts[3 * t.perm[i] + c];
+        const int cnt = t.u[k] - t.l[k] + 1;
+        for (int c = 0; c < 3; ++c) s[c] = s[c] / cnt;
+        double radius = 0;
+        for (int i = t.l[k]; i <= t.u[k]; ++i) {
+            double dx = pts[3 * t.perm[i]] - s[0], dy = pts[3 * t.perm[i] + 1] - s[1],
+                   dz = pts[3 * t.perm[i] + 2] - s[2];
+            radius = std::max(radius, std::sqrt(dx * dx + dy * dy + dz * dz));
+        }
+        for (int c = 0; c < 3; ++c) t.X[3 * k + c] = s[c];
+        t.oradius[k] = 1.0 / radius;
+    }
+}
+
+}  // namespace idw

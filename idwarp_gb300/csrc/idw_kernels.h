@@ -1,0 +1,107 @@
+// Device-side views and kernel launchers of the GB300 IDW warping library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "idw_common.cuh"
+
+namespace idw {
+
+// Surface connectivity in tree order (CSR), read-only after set-up.
+struct SurfaceDev {
+    int n;               // unique surface nodes
+    const int *facePtr;  // nFaces+1
+    const int *faceConn; // tree-order vertex ids
+    const int *n2ePtr;   // n+1
+    const int *n2e;      // node -> face ids (one entry per occurrence)
+};
+
+// Tree nodes in preorder.  info = (l, u, escape, isLeaf).
+struct TreeDev {
+    int nNodes;
+    const int4 *info;
+    const dbl4 *geom;  // X, oradius
+    const double *err;    // 12 per node
+    const double *ai;     // per node
+};
+
+// FP32 companion arrays of the mixed-precision path (set-up constants).
+struct TreeDevF {
+    const float4 *cHi;   // centroid high part, oradius
+    const float4 *cLo;   // centroid low part, node area A
+    const float *err;    // 12 per node (true weight units)
+};
+
+// Surface point data for the evaluation kernels, tree order.
+struct PointsDev {
+    const dbl4 *xa;   // Xu0, Ai (FP64)
+    const double *mb;    // 12 per point: M row-major, b
+};
+
+struct PointsDevF {
+    const float4 *da;    // Xu0 - centroid(leaf), Ai  (FP32, set-up constant)
+    const float *dm;     // 12 per point: D = M - I (9), u = M Xu0 + b - Xu0 (3)
+};
+
+struct NodeAggF {
+    const float *dc;     // 12 per node: Dbar = Mbar - I (9), c = Mbar X + bbar - X (3)
+};
+
+struct VolumeDev {
+    int64_t nVol;
+    const int *perm;       // Morton order -> common index
+    const double *xv0;     // (nVol,3) common order
+    const double *den0;    // denominator0, common order
+};
+
+struct WalkOut {
+    double *xv;            // (nVol,3) or nullptr
+    double *den;           // (nVol) true-unit denominators or nullptr
+    unsigned long long *counters;  // leafPairs, approx, visited, fp64Fallback
+};
+
+struct EvalConsts {
+    WeightLaw law;
+    double errTol;
+    SymPlanes sym;
+};
+
+// Nodal properties (idw_nodal.cu)
+void launch_gather_xu(int n, const int *xuInd, const double *Xs, double *Xu, cudaStream_t st);
+void launch_nodal_init(const SurfaceDev &s, const double *Xu, double *normals0, double *Ai, cudaStream_t st);
+void launch_corners(const SurfaceDev &s, const double *Xu, const double *normals0, double threshold, int enabled,
+                    int *isCorner, cudaStream_t st);
+void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
+                  const double *Ai, const int *isCorner, int useRotations, double *ptMB, cudaStream_t st);
+void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, cudaStream_t st);
+void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st);
+void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
+                    const int *isCorner, int useRotations, const double *ptAdj, double *Xub, cudaStream_t st);
+void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st);
+
+// Set-up kernels (idw_setup.cu)
+void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err,
+                           double *scratch, int64_t scratchLen, cudaStream_t st);
+void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
+                         const SymPlanes &sym, double *den0, cudaStream_t st);
+void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,
+                         unsigned long long *codes, int *idx, cudaStream_t st);
+void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, const double *nodeX,
+                         float4 *ptDA, cudaStream_t st);
+void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, cudaStream_t st);
+void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, cudaStream_t st);
+
+// Evaluation (idw_walk.cu)
+void launch_walk_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const double *nodeMB,
+                      const EvalConsts &k, int exact, int nPts, const WalkOut &o, cudaStream_t st);
+void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                       const VolumeDev &v, const EvalConsts &k, int exact, const WalkOut &o, cudaStream_t st);
+void launch_to_float(int64_t n, const double *src, float *dst, cudaStream_t st);
+int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,
+                             int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,
+                             double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
+                             unsigned long long *counters, cudaStream_t st);
+int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
+                cudaStream_t st);
+
+}  // namespace idw

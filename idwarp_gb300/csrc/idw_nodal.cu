@@ -1,0 +1,472 @@
+// Per-surface-node properties on the GPU (FP64):
+//   forward  computeNodalProperties   src/modules/kd_tree.F90:1580-1664
+//            getElementProps          src/warp/getElementProps.F90:1-46
+//            getRotationMatrix3d      src/utils/vectorUtils.f90:31-103
+//            determineCorners         src/modules/kd_tree.F90:1666-1715
+//            setData                  src/modules/kd_tree.F90:595-617
+//   reverse  COMPUTENODALPROPERTIES_B src/modules/kd_tree.F90:1057-1162
+//            setData_b                src/modules/kd_tree.F90:1033-1051
+// The reverse kernels recompute the forward intermediates of each node in
+// registers instead of replaying a tape.
+#include "idw_common.cuh"
+#include "idw_kernels.h"
+
+namespace idw {
+
+namespace {
+
+__device__ __forceinline__ void cross3(const double *a, const double *b, double *c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Area and unit normal of one polygonal face (fan of cross products of the
+// centre-relative vertex vectors).
+__device__ void element_props(const double *Xu, const int *conn, int np, double &area, double *normal) {
+    double c[3] = {0, 0, 0};
+    for (int k = 0; k < np; ++k) {
+        const double *p = Xu + 3 * conn[k];
+        c[0] += p[0];
+        c[1] += p[1];
+        c[2] += p[2];
+    }
+    c[0] /= double(np);
+    c[1] /= double(np);
+    c[2] /= double(np);
+    double nrm[3] = {0, 0, 0};
+    double a = 0;
+    const double *p0 = Xu + 3 * conn[0];
+    double rv0[3] = {p0[0] - c[0], p0[1] - c[1], p0[2] - c[2]};
+    double rvi[3] = {rv0[0], rv0[1], rv0[2]};
+    for (int k = 0; k < np; ++k) {
+        double rvj[3];
+        if (k < np - 1) {
+            const double *pj = Xu + 3 * conn[k + 1];
+            rvj[0] = pj[0] - c[0];
+            rvj[1] = pj[1] - c[1];
+            rvj[2] = pj[2] - c[2];
+        } else {
+            rvj[0] = rv0[0];
+            rvj[1] = rv0[1];
+            rvj[2] = rv0[2];
+        }
+        double cr[3];
+        cross3(rvi, rvj, cr);
+        double cn = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2] + 1e-15);
+        a += 0.5 * cn;
+        nrm[0] += cr[0] / cn;
+        nrm[1] += cr[1] / cn;
+        nrm[2] += cr[2] / cn;
+        rvi[0] = rvj[0];
+        rvi[1] = rvj[1];
+        rvi[2] = rvj[2];
+    }
+    double m = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+    normal[0] = nrm[0] / m;
+    normal[1] = nrm[1] / m;
+    normal[2] = nrm[2] / m;
+    area = a;
+}
+
+// Adjoint of element_props: accumulate d(area)*areab + d(normal).normalb into
+// Xub of the face's vertices (atomically: vertices are shared between nodes).
+__device__ void element_props_b(const double *Xu, const int *conn, int np, double areab, const double *normalb,
+                                double *Xub) {
+    double c[3] = {0, 0, 0};
+    for (int k = 0; k < np; ++k) {
+        const double *p = Xu + 3 * conn[k];
+        c[0] += p[0];
+        c[1] += p[1];
+        c[2] += p[2];
+    }
+    c[0] /= double(np);
+    c[1] /= double(np);
+    c[2] /= double(np);
+    auto rv = [&](int k, double *o) {
+        const double *p = Xu + 3 * conn[k];
+        o[0] = p[0] - c[0];
+        o[1] = p[1] - c[1];
+        o[2] = p[2] - c[2];
+    };
+    // forward pass: the un-normalised normal sum
+    double ns[3] = {0, 0, 0};
+    for (int k = 0; k < np; ++k) {
+        double a[3], b[3], cr[3];
+        rv(k, a);
+        rv(k < np - 1 ? k + 1 : 0, b);
+        cross3(a, b, cr);
+        double cn = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2] + 1e-15);
+        ns[0] += cr[0] / cn;
+        ns[1] += cr[1] / cn;
+        ns[2] += cr[2] / cn;
+    }
+    double t = ns[0] * ns[0] + ns[1] * ns[1] + ns[2] * ns[2];
+    double t0 = sqrt(t);
+    double dotb = ns[0] * normalb[0] + ns[1] * normalb[1] + ns[2] * normalb[2];
+    double tb = (t == 0.0) ? 0.0 : -(dotb / (2.0 * t0 * t0 * t0));
+    double nsb[3] = {normalb[0] / t0 + 2 * ns[0] * tb, normalb[1] / t0 + 2 * ns[1] * tb,
+                     normalb[2] / t0 + 2 * ns[2] * tb};
+    double rvb[kMaxFacePts][3];
+    for (int k = 0; k < np; ++k) rvb[k][0] = rvb[k][1] = rvb[k][2] = 0.0;
+    for (int k = np - 1; k >= 0; --k) {
+        int j = k < np - 1 ? k + 1 : 0;
+        double a[3], b[3], cr[3];
+        rv(k, a);
+        rv(j, b);
+        cross3(a, b, cr);
+        double cn = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2] + 1e-15);
+        double crb[3] = {nsb[0] / cn, nsb[1] / cn, nsb[2] / cn};
+        double cnb = 0.5 * areab - (cr[0] * nsb[0] + cr[1] * nsb[1] + cr[2] * nsb[2]) / (cn * cn);
+        double q = cnb / (2.0 * cn);
+        crb[0] += 2 * cr[0] * q;
+        crb[1] += 2 * cr[1] * q;
+        crb[2] += 2 * cr[2] * q;
+        double tmp[3];
+        cross3(b, crb, tmp);  // d(a x b)/da applied to crb
+        rvb[k][0] += tmp[0];
+        rvb[k][1] += tmp[1];
+        rvb[k][2] += tmp[2];
+        cross3(crb, a, tmp);  // d(a x b)/db applied to crb
+        rvb[j][0] += tmp[0];
+        rvb[j][1] += tmp[1];
+        rvb[j][2] += tmp[2];
+    }
+    double cb[3] = {0, 0, 0};
+    for (int k = 0; k < np; ++k) {
+        cb[0] -= rvb[k][0];
+        cb[1] -= rvb[k][1];
+        cb[2] -= rvb[k][2];
+    }
+    cb[0] /= double(np);
+    cb[1] /= double(np);
+    cb[2] /= double(np);
+    for (int k = 0; k < np; ++k) {
+        double *o = Xub + 3 * conn[k];
+        atomicAdd(o + 0, rvb[k][0] + cb[0]);
+        atomicAdd(o + 1, rvb[k][1] + cb[1]);
+        atomicAdd(o + 2, rvb[k][2] + cb[2]);
+    }
+}
+
+__device__ __forceinline__ double mag_eps(const double *v) {
+    return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + 1e-30);
+}
+
+constexpr double kRotTol = 1.4901161193847656e-08;
+
+// Rodrigues rotation taking direction v1 to direction v2 (row-major M).
+__device__ void rotation_matrix(const double *v1, const double *v2, double *M) {
+    double mag1 = mag_eps(v1), mag2 = mag_eps(v2);
+    double ax[3];
+    cross3(v1, v2, ax);
+    double axm = mag_eps(ax);
+    double s, omc;
+    if (axm < kRotTol) {
+        ax[0] = 1.0;
+        ax[1] = 0.0;
+        ax[2] = 0.0;
+        s = 0.0;
+        omc = 0.0;
+    } else {
+        ax[0] /= axm;
+        ax[1] /= axm;
+        ax[2] /= axm;
+        double d = (v1[0] / mag1) * (v2[0] / mag2) + (v1[1] / mag1) * (v2[1] / mag2) + (v1[2] / mag1) * (v2[2] / mag2);
+        double arg = (1.0 > d) ? d : 1.0;
+        double ang = acos(arg);
+        s = sin(ang);
+        omc = 1.0 - cos(ang);
+    }
+    double A[9] = {0.0, -ax[2], ax[1], ax[2], 0.0, -ax[0], -ax[1], ax[0], 0.0};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double C = A[3 * i] * A[j] + A[3 * i + 1] * A[3 + j] + A[3 * i + 2] * A[6 + j];
+            M[3 * i + j] = (i == j ? 1.0 : 0.0) + s * A[3 * i + j] + omc * C;
+        }
+}
+
+// Adjoint of rotation_matrix with respect to v2 (v1 = normals0 is fixed).
+// Zero when the rotation axis is degenerate (axisMag < tol) or the acos
+// argument was clamped, as the reference's derivative
+// (src/adjoint/outputReverse/vectorUtils_b.f90:7-154).
+__device__ void rotation_matrix_b(const double *v1, const double *v2, const double *Mb, double *v2b) {
+    double mag1 = mag_eps(v1), mag2 = mag_eps(v2);
+    double ax0[3];
+    cross3(v1, v2, ax0);
+    double axm = mag_eps(ax0);
+    if (axm < kRotTol) return;
+    double ax[3] = {ax0[0] / axm, ax0[1] / axm, ax0[2] / axm};
+    double vv1[3] = {v1[0] / mag1, v1[1] / mag1, v1[2] / mag1};
+    double d = vv1[0] * (v2[0] / mag2) + vv1[1] * (v2[1] / mag2) + vv1[2] * (v2[2] / mag2);
+    bool clamped = !(1.0 > d);
+    double arg = clamped ? 1.0 : d;
+    double ang = acos(arg);
+    double s = sin(ang), c = cos(ang);
+    double A[9] = {0.0, -ax[2], ax[1], ax[2], 0.0, -ax[0], -ax[1], ax[0], 0.0};
+    double angb = 0.0;
+    double Ab[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double C = A[3 * i] * A[j] + A[3 * i + 1] * A[3 + j] + A[3 * i + 2] * A[6 + j];
+            angb += c * A[3 * i + j] * Mb[3 * i + j] + s * C * Mb[3 * i + j];
+            Ab[3 * i + j] = s * Mb[3 * i + j];
+        }
+    const double w = 1.0 - c;  // Cb = w * Mb; Ab += Cb A^T + A^T Cb
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc += Mb[3 * i + k] * A[3 * j + k] + A[3 * k + i] * Mb[3 * k + j];
+            Ab[3 * i + j] += w * acc;
+        }
+    double axb[3] = {Ab[7] - Ab[5], Ab[2] - Ab[6], Ab[3] - Ab[1]};
+    double argb = (arg == 1.0 || arg == -1.0) ? 0.0 : -(angb / sqrt(1.0 - arg * arg));
+    double vv2b[3] = {0, 0, 0};
+    if (!clamped) {
+        vv2b[0] = vv1[0] * argb;
+        vv2b[1] = vv1[1] * argb;
+        vv2b[2] = vv1[2] * argb;
+    }
+    double mag2b = -(v2[0] * vv2b[0] + v2[1] * vv2b[1] + v2[2] * vv2b[2]) / (mag2 * mag2);
+    double axmb = -(ax0[0] * axb[0] + ax0[1] * axb[1] + ax0[2] * axb[2]) / (axm * axm);
+    double ax0b[3] = {axb[0] / axm + ax0[0] * axmb / axm, axb[1] / axm + ax0[1] * axmb / axm,
+                      axb[2] / axm + ax0[2] * axmb / axm};
+    double tmp[3];
+    cross3(ax0b, v1, tmp);  // ax0 = v1 x v2
+    v2b[0] += vv2b[0] / mag2 + tmp[0] + v2[0] * mag2b / mag2;
+    v2b[1] += vv2b[1] / mag2 + tmp[1] + v2[1] * mag2b / mag2;
+    v2b[2] += vv2b[2] / mag2 + tmp[2] + v2[2] * mag2b / mag2;
+}
+
+// Area-weighted node normal from the node's faces (kd_tree.F90:1603-1625).
+__device__ void node_normal(const SurfaceDev &s, const double *Xu, int i, double &sumArea, double *sumNormal) {
+    sumArea = 0.0;
+    sumNormal[0] = sumNormal[1] = sumNormal[2] = 0.0;
+    for (int e = s.n2ePtr[i]; e < s.n2ePtr[i + 1]; ++e) {
+        int f = s.n2e[e];
+        int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
+        double area, fn[3];
+        element_props(Xu, s.faceConn + f0, np, area, fn);
+        double dA = area / double(np);
+        sumArea += dA;
+        sumNormal[0] += dA * fn[0];
+        sumNormal[1] += dA * fn[1];
+        sumNormal[2] += dA * fn[2];
+    }
+}
+
+__global__ void k_gather_xu(int n, const int *xuInd, const double *Xs, double *Xu) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int j = xuInd[i];
+    Xu[3 * i + 0] = Xs[3 * j + 0];
+    Xu[3 * i + 1] = Xs[3 * j + 1];
+    Xu[3 * i + 2] = Xs[3 * j + 2];
+}
+
+// Initial pass: normals0 and the node areas Ai (kd_tree.F90:1630-1636).
+__global__ void k_nodal_init(SurfaceDev s, const double *Xu, double *normals0, double *Ai) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    double sa, sn[3];
+    node_normal(s, Xu, i, sa, sn);
+    normals0[3 * i + 0] = sn[0] / sa;
+    normals0[3 * i + 1] = sn[1] / sa;
+    normals0[3 * i + 2] = sn[2] / sa;
+    Ai[i] = sa;
+}
+
+__global__ void k_corners(SurfaceDev s, const double *Xu, const double *normals0, double threshold, int enabled,
+                          int *isCorner) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    int flag = 0;
+    if (enabled) {
+        for (int e = s.n2ePtr[i]; e < s.n2ePtr[i + 1]; ++e) {
+            int f = s.n2e[e];
+            int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
+            double area, fn[3];
+            element_props(Xu, s.faceConn + f0, np, area, fn);
+            double dp = fn[0] * normals0[3 * i] + fn[1] * normals0[3 * i + 1] + fn[2] * normals0[3 * i + 2];
+            if (fabs(dp) < threshold) flag = 1;
+        }
+    }
+    isCorner[i] = flag;
+}
+
+// Per warp: Mi, Bi of every node (kd_tree.F90:1637-1663), stored as 12
+// doubles per node (M row-major, then b).
+__global__ void k_nodal(SurfaceDev s, const double *Xu, const dbl4 *xa, const double *normals0, const double *Ai,
+                        const int *isCorner, int useRotations, double *ptMB) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    double M[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    double b[3] = {0, 0, 0};
+    if (Ai[i] != 0.0) {
+        if (useRotations && !isCorner[i]) {
+            double sa, sn[3];
+            node_normal(s, Xu, i, sa, sn);
+            double nrm[3] = {sn[0] / sa, sn[1] / sa, sn[2] / sa};
+            rotation_matrix(normals0 + 3 * i, nrm, M);
+        }
+        const dbl4 q = xa[i];
+        const double x0[3] = {q.x, q.y, q.z};
+        for (int a = 0; a < 3; ++a)
+            b[a] = Xu[3 * i + a] - (M[3 * a] * x0[0] + M[3 * a + 1] * x0[1] + M[3 * a + 2] * x0[2]);
+    }
+    double *o = ptMB + 12 * i;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) o[q] = M[q];
+    o[9] = b[0];
+    o[10] = b[1];
+    o[11] = b[2];
+}
+
+// setData: unweighted mean of the 12 node values over each interior node's
+// range; one block per interior node.
+__global__ void k_set_data(TreeDev t, const double *ptMB, double *nodeMB) {
+    int q = blockIdx.x;
+    if (q >= t.nNodes) return;
+    int4 inf = t.info[q];
+    if (inf.w) return;  // leaves carry no aggregate
+    double acc[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) acc[c] = 0.0;
+    for (int i = inf.x + threadIdx.x; i <= inf.y; i += blockDim.x) {
+        const double *p = ptMB + 12 * i;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) acc[c] += p[c];
+    }
+    __shared__ double red[12][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) {
+        double v = warp_sum(acc[c]);
+        if (lane == 0) red[c][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 12) {
+        double v = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+        nodeMB[12 * q + threadIdx.x] = v / double(inf.y - inf.x + 1);
+    }
+}
+
+// setData_b: push the cluster adjoints down to the member points
+// (kd_tree.F90:1033-1051).  One thread per point walks its ancestors.
+__global__ void k_set_data_b(TreeDev t, const double *nodeAdj, double *ptAdj, int nPts) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nPts) return;
+    double acc[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) acc[c] = 0.0;
+    int q = 0;
+    while (q < t.nNodes) {
+        int4 inf = t.info[q];
+        if (inf.w) break;
+        double ovrN = 1.0 / double(inf.y - inf.x + 1);
+        const double *a = nodeAdj + 12 * q;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) acc[c] += a[c] * ovrN;
+        int left = q + 1;
+        int4 li = t.info[left];
+        q = (i <= li.y) ? left : li.z;
+    }
+    double *o = ptAdj + 12 * i;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) o[c] += acc[c];
+}
+
+// Reverse nodal properties: point adjoints (Mib, Bib) -> Xub; one thread per
+// node, scatter to face vertices with atomics.
+__global__ void k_nodal_b(SurfaceDev s, const double *Xu, const dbl4 *xa, const double *normals0,
+                          const int *isCorner, int useRotations, const double *ptAdj, double *Xub) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    const double *adj = ptAdj + 12 * i;
+    double Mb[9];
+    double Bb[3] = {adj[9], adj[10], adj[11]};
+    atomicAdd(Xub + 3 * i + 0, Bb[0]);
+    atomicAdd(Xub + 3 * i + 1, Bb[1]);
+    atomicAdd(Xub + 3 * i + 2, Bb[2]);
+    if (!(useRotations && !isCorner[i])) return;
+    const int e0 = s.n2ePtr[i], e1 = s.n2ePtr[i + 1];
+    if (e1 == e0) return;
+    const dbl4 q = xa[i];
+    const double x0[3] = {q.x, q.y, q.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Mb[3 * a + k] = adj[3 * a + k] - x0[k] * Bb[a];
+    double sa, sn[3];
+    node_normal(s, Xu, i, sa, sn);
+    double nrm[3] = {sn[0] / sa, sn[1] / sa, sn[2] / sa};
+    double nb[3] = {0, 0, 0};
+    rotation_matrix_b(normals0 + 3 * i, nrm, Mb, nb);
+    double snb[3] = {nb[0] / sa, nb[1] / sa, nb[2] / sa};
+    double sab = -(sn[0] * nb[0] + sn[1] * nb[1] + sn[2] * nb[2]) / sa / sa;
+    for (int e = e1 - 1; e >= e0; --e) {
+        int f = s.n2e[e];
+        int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
+        double area, fn[3];
+        element_props(Xu, s.faceConn + f0, np, area, fn);
+        double dA = area / double(np);
+        double dAb = sab + fn[0] * snb[0] + fn[1] * snb[1] + fn[2] * snb[2];
+        double fnb[3] = {dA * snb[0], dA * snb[1], dA * snb[2]};
+        element_props_b(Xu, s.faceConn + f0, np, dAb / double(np), fnb, Xub);
+    }
+}
+
+// dXs[XuInd[i]] = Xub[i]: only the first caller occurrence of a unique point
+// receives the gradient (kd_tree.F90:1155-1159); dXs is pre-zeroed.
+__global__ void k_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int j = xuInd[i];
+    dXs[3 * j + 0] = Xub[3 * i + 0];
+    dXs[3 * j + 1] = Xub[3 * i + 1];
+    dXs[3 * j + 2] = Xub[3 * i + 2];
+}
+
+inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
+
+}  // namespace
+
+void launch_gather_xu(int n, const int *xuInd, const double *Xs, double *Xu, cudaStream_t st) {
+    if (n > 0) k_gather_xu<<<blocks(n, 256), 256, 0, st>>>(n, xuInd, Xs, Xu);
+}
+void launch_nodal_init(const SurfaceDev &s, const double *Xu, double *normals0, double *Ai, cudaStream_t st) {
+    if (s.n > 0) k_nodal_init<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, normals0, Ai);
+}
+void launch_corners(const SurfaceDev &s, const double *Xu, const double *normals0, double threshold, int enabled,
+                    int *isCorner, cudaStream_t st) {
+    if (s.n > 0) k_corners<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, normals0, threshold, enabled, isCorner);
+}
+void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
+                  const double *Ai, const int *isCorner, int useRotations, double *ptMB, cudaStream_t st) {
+    if (s.n > 0)
+        k_nodal<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, Ai, isCorner, useRotations, ptMB);
+}
+void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, cudaStream_t st) {
+    if (t.nNodes > 0) k_set_data<<<t.nNodes, 128, 0, st>>>(t, ptMB, nodeMB);
+}
+void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st) {
+    if (nPts > 0) k_set_data_b<<<blocks(nPts, 128), 128, 0, st>>>(t, nodeAdj, ptAdj, nPts);
+}
+void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
+                    const int *isCorner, int useRotations, const double *ptAdj, double *Xub, cudaStream_t st) {
+    if (s.n > 0)
+        k_nodal_b<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, isCorner, useRotations, ptAdj, Xub);
+}
+void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st) {
+    if (n > 0) k_scatter_dxs<<<blocks(n, 256), 256, 0, st>>>(n, xuInd, Xub, dXs);
+}
+
+}  // namespace idw

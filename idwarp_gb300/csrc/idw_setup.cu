@@ -1,0 +1,339 @@
+// Set-up kernels: error tables, denominator estimate, Morton ordering of the
+// volume nodes and the FP32 companion arrays of the mixed-precision path.
+//   computeErrors  src/modules/kd_tree.F90:832-880 (+ getSpherePts, src/utils/getSpherePts.F90)
+//   getWiEstimate  src/modules/kd_tree.F90:751-787, driven by src/warp/initializeWarping.F90:241-247
+#include <cub/cub.cuh>
+
+#include <vector>
+
+#include "idw_common.cuh"
+#include "idw_kernels.h"
+
+namespace idw {
+
+namespace {
+
+// Dodecahedron vertices before scaling (src/utils/getSpherePts.F90:16-39);
+// phi = 2.1180339887498949 as in src/modules/constants.F90:32.
+__device__ __forceinline__ void sphere_vertex(int ii, double *v) {
+    const double p = 2.1180339887498949, ip = 1.0 / 2.1180339887498949;
+    const double o = 1.0;
+    switch (ii) {
+        case 0: v[0] = -o; v[1] = -o; v[2] = -o; break;
+        case 1: v[0] = o; v[1] = -o; v[2] = -o; break;
+        case 2: v[0] = -o; v[1] = o; v[2] = -o; break;
+        case 3: v[0] = o; v[1] = o; v[2] = -o; break;
+        case 4: v[0] = -o; v[1] = -o; v[2] = o; break;
+        case 5: v[0] = o; v[1] = -o; v[2] = o; break;
+        case 6: v[0] = -o; v[1] = o; v[2] = o; break;
+        case 7: v[0] = o; v[1] = o; v[2] = o; break;
+        case 8: v[0] = 0; v[1] = -ip; v[2] = -p; break;
+        case 9: v[0] = 0; v[1] = ip; v[2] = -p; break;
+        case 10: v[0] = 0; v[1] = -ip; v[2] = p; break;
+        case 11: v[0] = 0; v[1] = ip; v[2] = p; break;
+        case 12: v[0] = -ip; v[1] = -p; v[2] = 0; break;
+        case 13: v[0] = ip; v[1] = -p; v[2] = 0; break;
+        case 14: v[0] = -ip; v[1] = p; v[2] = 0; break;
+        case 15: v[0] = ip; v[1] = p; v[2] = 0; break;
+        case 16: v[0] = -p; v[1] = 0; v[2] = -ip; break;
+        case 17: v[0] = -p; v[1] = 0; v[2] = ip; break;
+        case 18: v[0] = p; v[1] = 0; v[2] = -ip; break;
+        default: v[0] = p; v[1] = 0; v[2] = ip; break;
+    }
+}
+
+__device__ __forceinline__ void sphere_point(const dbl4 &g, int t, double *pt) {
+    // t = 20*j + ii: radius (1/oradius)*rstar(j), vertex ii
+    int j = t / 20, ii = t - 20 * j;
+    double v[3];
+    sphere_vertex(ii, v);
+    double radius = (1.0 / g.w) * c_rstar[j];
+    double s = radius / sqrt(3.0);
+    pt[0] = v[0] * s + g.x;
+    pt[1] = v[1] * s + g.y;
+    pt[2] = v[2] * s + g.z;
+}
+
+struct ErrItem {
+    int node, i0, i1, pad;
+};
+
+constexpr int kErrChunk = 512;
+
+// Partial exact sums over one chunk of one node's members for its 240 probe
+// points.
+__global__ void k_err_partial(TreeDev t, const dbl4 *ptXA, WeightLaw law, const ErrItem *items, double *part) {
+    const ErrItem it = items[blockIdx.x];
+    const dbl4 g = t.geom[it.node];
+    __shared__ dbl4 sx[256];
+    const int tid = threadIdx.x;
+    double pt[3] = {0, 0, 0};
+    if (tid < 240) sphere_point(g, tid, pt);
+    double acc = 0.0;
+    for (int base = it.i0; base < it.i1; base += 256) {
+        int m = min(256, it.i1 - base);
+        __syncthreads();
+        if (tid < m) sx[tid] = ptXA[base + tid];
+        __syncthreads();
+        if (tid < 240) {
+            for (int k = 0; k < m; ++k) {
+                dbl4 x = sx[k];
+                double r0 = pt[0] - x.x, r1 = pt[1] - x.y, r2 = pt[2] - x.z;
+                double dist = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+                acc += x.w * law64(law, law.Ldef / dist);
+            }
+        }
+    }
+    if (tid < 240) part[(int64_t)blockIdx.x * 240 + tid] = acc;
+}
+
+__global__ void k_err_final(TreeDev t, WeightLaw law, const int *nodeItem0, const int *interior, const double *part,
+                            double *err) {
+    const int q = interior[blockIdx.x];
+    const int tid = threadIdx.x;
+    __shared__ double sq[240];
+    if (tid < 240) {
+        int a = nodeItem0[blockIdx.x], b = nodeItem0[blockIdx.x + 1];
+        double dExact = 0.0;
+        for (int k = a; k < b; ++k) dExact += part[(int64_t)k * 240 + tid];
+        const dbl4 g = t.geom[q];
+        double pt[3];
+        sphere_point(g, tid, pt);
+        double r0 = pt[0] - g.x, r1 = pt[1] - g.y, r2 = pt[2] - g.z;
+        double dist = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+        double dApprox = t.ai[q] * law64(law, law.Ldef / dist);
+        double d = dExact - dApprox;
+        sq[tid] = d * d;
+    }
+    __syncthreads();
+    if (tid < kNerr) {
+        double s = 0.0;
+        for (int ii = 0; ii < 20; ++ii) s += sq[20 * tid + ii];
+        err[(int64_t)kNerr * q + tid] = sqrt(s / 20);
+    }
+}
+
+// Denominator estimate: warp-cooperative walk with the 5-radius far-field
+// rule; every lane follows exactly its own recursion of getWiEstimate.
+__global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, SymPlanes sym, double *den0) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool valid = gid < v.nVol;
+    const int vi = valid ? v.perm[gid] : 0;
+    double x0[3] = {v.xv0[3 * vi], v.xv0[3 * vi + 1], v.xv0[3 * vi + 2]};
+    double acc = 0.0;
+    for (int kk = 0; kk < sym.nLoop; ++kk) {
+        double r[3];
+        mirror_point(sym, kk, x0, r);
+        int node = 0, skip = 0;
+        while (node < t.nNodes) {
+            const int4 inf = t.info[node];
+            const bool active = valid && node >= skip;
+            if (inf.w) {
+                if (active) {
+                    for (int i = inf.x; i <= inf.y; ++i) {
+                        dbl4 x = ptXA[i];
+                        double r0 = r[0] - x.x, r1 = r[1] - x.y, r2 = r[2] - x.z;
+                        double LoD = law.Ldef / sqrt(r0 * r0 + r1 * r1 + r2 * r2 + 1e-16);
+                        acc += x.w * law64(law, LoD);
+                    }
+                }
+                node = inf.z;
+            } else {
+                bool open = false;
+                if (active) {
+                    const dbl4 g = t.geom[node];
+                    double r0 = r[0] - g.x, r1 = r[1] - g.y, r2 = r[2] - g.z;
+                    double dist = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + 1e-16);
+                    if (dist * g.w > 5.0) {
+                        acc += t.ai[node] * law64(law, law.Ldef / dist);
+                        skip = inf.z;
+                    } else {
+                        open = true;
+                    }
+                }
+                node = __any_sync(kFull, open) ? node + 1 : inf.z;
+            }
+        }
+    }
+    if (valid) den0[vi] = acc;
+}
+
+__device__ __forceinline__ unsigned long long spread21(unsigned long long x) {
+    x &= 0x1fffffull;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(int64_t n, const double *xv0, double lo0, double lo1, double lo2, double s0, double s1,
+                         double s2, unsigned long long *codes, int *idx) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double f[3] = {(xv0[3 * i] - lo0) * s0, (xv0[3 * i + 1] - lo1) * s1, (xv0[3 * i + 2] - lo2) * s2};
+    unsigned long long q[3];
+    for (int k = 0; k < 3; ++k) {
+        double c = fmin(fmax(f[k], 0.0), 2097151.0);
+        q[k] = (unsigned long long)c;
+    }
+    codes[i] = spread21(q[0]) | (spread21(q[1]) << 1) | (spread21(q[2]) << 2);
+    idx[i] = int(i);
+}
+
+// Point offsets from the centroid of their leaf (set-up constant, FP32).
+__global__ void k_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *geom, const dbl4 *ptXA,
+                               float4 *ptDA) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int q = 0;
+    while (q < nNodes) {
+        int4 inf = info[q];
+        if (inf.w) break;
+        int4 li = info[q + 1];
+        q = (i <= li.y) ? q + 1 : li.z;
+    }
+    dbl4 g = geom[q];
+    dbl4 x = ptXA[i];
+    ptDA[i] = make_float4(float(x.x - g.x), float(x.y - g.y), float(x.z - g.z), float(x.w));
+}
+
+// Per warp: D = M - I and u = M Xu0 + b - Xu0 per point, in FP32.
+__global__ void k_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *m = ptMB + 12 * i;
+    dbl4 x = ptXA[i];
+    float *o = ptDM + 12 * i;
+    double X[3] = {x.x, x.y, x.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double Mx = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double d = m[3 * a + k] - (a == k ? 1.0 : 0.0);
+            o[3 * a + k] = float(d);
+            Mx += d * X[k];
+        }
+        o[9 + a] = float(Mx + m[9 + a]);
+    }
+}
+
+// Per warp: cluster Dbar = Mbar - I and c = Mbar X + bbar - X in FP32
+// (interior nodes only; leaves are never approximated).
+__global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, float *nodeDC) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= t.nNodes) return;
+    if (t.info[q].w) return;
+    const double *m = nodeMB + 12 * q;
+    dbl4 g = t.geom[q];
+    double X[3] = {g.x, g.y, g.z};
+    float *o = nodeDC + 12 * q;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        double Mx = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double d = m[3 * a + k] - (a == k ? 1.0 : 0.0);
+            o[3 * a + k] = float(d);
+            Mx += d * X[k];
+        }
+        o[9 + a] = float(Mx + m[9 + a]);
+    }
+}
+
+__global__ void k_to_float(int64_t n, const double *src, float *dst) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = float(src[i]);
+}
+
+inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
+
+}  // namespace
+
+void launch_to_float(int64_t n, const double *src, float *dst, cudaStream_t st) {
+    if (n > 0) k_to_float<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
+}
+
+void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err,
+                           double *scratch, int64_t scratchLen, cudaStream_t st) {
+    (void)scratch;
+    (void)scratchLen;
+    // Build the (node, chunk) work list on the host.
+    std::vector<int4> info(t.nNodes);
+    cudaMemcpyAsync(info.data(), t.info, sizeof(int4) * t.nNodes, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    std::vector<ErrItem> items;
+    std::vector<int> item0, interior;
+    for (int q = 0; q < t.nNodes; ++q) {
+        if (info[q].w) continue;
+        interior.push_back(q);
+        item0.push_back(int(items.size()));
+        for (int a = info[q].x; a <= info[q].y; a += kErrChunk) items.push_back({q, a, min(a + kErrChunk, info[q].y + 1), 0});
+    }
+    item0.push_back(int(items.size()));
+    cudaMemsetAsync(err, 0, sizeof(double) * kNerr * t.nNodes, st);
+    if (interior.empty()) return;
+    ErrItem *dItems;
+    int *dItem0, *dInterior;
+    double *dPart;
+    cudaMalloc(&dItems, sizeof(ErrItem) * items.size());
+    cudaMalloc(&dItem0, sizeof(int) * item0.size());
+    cudaMalloc(&dInterior, sizeof(int) * interior.size());
+    cudaMalloc(&dPart, sizeof(double) * 240 * items.size());
+    cudaMemcpyAsync(dItems, items.data(), sizeof(ErrItem) * items.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dItem0, item0.data(), sizeof(int) * item0.size(), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dInterior, interior.data(), sizeof(int) * interior.size(), cudaMemcpyHostToDevice, st);
+    k_err_partial<<<int(items.size()), 256, 0, st>>>(t, ptXA, law, dItems, dPart);
+    k_err_final<<<int(interior.size()), 256, 0, st>>>(t, law, dItem0, dInterior, dPart, err);
+    cudaStreamSynchronize(st);
+    cudaFree(dItems);
+    cudaFree(dItem0);
+    cudaFree(dInterior);
+    cudaFree(dPart);
+}
+
+void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
+                         const SymPlanes &sym, double *den0, cudaStream_t st) {
+    if (v.nVol > 0) k_den0<<<blocks(v.nVol, 128), 128, 0, st>>>(t, ptXA, v, law, sym, den0);
+}
+
+void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,
+                         unsigned long long *codes, int *idx, cudaStream_t st) {
+    double s[3];
+    for (int k = 0; k < 3; ++k) s[k] = (hi[k] > lo[k]) ? 2097151.0 / (hi[k] - lo[k]) : 0.0;
+    if (nVol > 0)
+        k_morton<<<blocks(nVol, 256), 256, 0, st>>>(nVol, xv0, lo[0], lo[1], lo[2], s[0], s[1], s[2], codes, idx);
+}
+
+void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, const double *nodeX,
+                         float4 *ptDA, cudaStream_t st) {
+    if (n > 0)
+        k_mixed_points<<<blocks(n, 256), 256, 0, st>>>(n, info, nNodes, reinterpret_cast<const dbl4 *>(nodeX),
+                                                        ptXA, ptDA);
+}
+
+void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, cudaStream_t st) {
+    if (n > 0) k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, ptXA, ptMB, ptDM);
+}
+
+void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, cudaStream_t st) {
+    if (t.nNodes > 0) k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, nodeDC);
+}
+
+// Sort volume nodes by Morton code (set-up).  perm[k] = common index of the
+// k-th node in Morton order.
+int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
+                cudaStream_t st) {
+    size_t tmp = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp, codes, codesAlt, idx, perm, (int)nVol, 0, 63, st);
+    void *dTmp = nullptr;
+    if (cudaMalloc(&dTmp, tmp) != cudaSuccess) return -1;
+    cub::DeviceRadixSort::SortPairs(dTmp, tmp, codes, codesAlt, idx, perm, (int)nVol, 0, 63, st);
+    cudaStreamSynchronize(st);
+    cudaFree(dTmp);
+    return 0;
+}
+
+}  // namespace idw

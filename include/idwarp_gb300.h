@@ -1,0 +1,198 @@
+/*
+ * idwarp_gb300.h — C ABI of the GB300 inverse-distance-weighted mesh-warping
+ * library (libidwarp_gb300.so).
+ *
+ * This ABI replaces the f2py module `libidwarp` of IDWarp (mdolab/idwarp,
+ * src/f2py/libidwarp.pyf) for the warping path: one opaque context per mesh
+ * instance (the reference instead copies the shared object per instance,
+ * idwarp/MExt.py:34-55), plain pointers and sizes, an int status on every
+ * call (0 = success, negative = error; the message is available through
+ * idw_last_error).  The reference aborts the MPI job on error
+ * (src/utils/EChk.F90:13-23).
+ *
+ * Coordinates are xyz-interleaved doubles, i.e. a C-order (N,3) array, which
+ * is the Fortran (3,N) layout the reference uses.  Index arrays are 0-based
+ * int32 except `link`, which is 1-based as in the reference.
+ *
+ * Pointers marked `where` may be host (IDW_HOST) or CUDA device (IDW_DEVICE)
+ * memory on the context's device.  All work is issued on the context's CUDA
+ * stream (idw_set_stream); calls taking host buffers synchronise that stream
+ * before returning.
+ *
+ * Thread safety: distinct contexts may be used from different threads; one
+ * context must not be used concurrently.
+ */
+#ifndef IDWARP_GB300_H
+#define IDWARP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IDW_OK 0
+#define IDW_ERR_ARG -1       /* bad argument (size mismatch, null pointer, bad option) */
+#define IDW_ERR_STATE -2     /* call made in the wrong order */
+#define IDW_ERR_CUDA -3      /* a CUDA runtime call failed */
+#define IDW_ERR_NONFINITE -4 /* non-finite coordinates detected */
+#define IDW_ERR_LIMIT -5     /* a fixed limit was exceeded (face size, symmetry planes) */
+#define IDW_ERR_NOMEM -6     /* device allocation failed */
+
+#define IDW_HOST 0
+#define IDW_DEVICE 1
+
+#define IDW_EVAL_EXACT 0 /* gridInput.f90:16 EVAL_EXACT */
+#define IDW_EVAL_FAST 1  /* gridInput.f90:17 EVAL_FAST */
+
+#define IDW_PREC_FP64 0  /* FP64 throughout (the plain form) */
+#define IDW_PREC_MIXED 1 /* FP32 distances/weights/accumulation, FP64 set-up and normalisation */
+
+/* Mesh options: the gridinput module variables (src/modules/gridInput.f90:9-18,
+ * libidwarp.pyf:148-162) plus kd_tree.bucket_size (libidwarp.pyf:204-206) and
+ * the GB300 precision switch.  Semantics follow doc/options.yaml. */
+typedef struct idw_options {
+    double aExp;          /* default 3 */
+    double bExp;          /* default 5 */
+    double LdefFact;      /* default 1 */
+    double alpha;         /* default 0.25 */
+    double errTol;        /* default 5e-4 */
+    double symmTol;       /* default 1e-6 (kept for API parity) */
+    double cornerAngle;   /* default 30 (degrees) */
+    int32_t evalMode;     /* IDW_EVAL_FAST (default) or IDW_EVAL_EXACT */
+    int32_t useRotations; /* default 1 */
+    int32_t zeroCornerRotations; /* default 1 */
+    int32_t bucketSize;   /* default 8 */
+    int32_t precision;    /* IDW_PREC_MIXED (default) or IDW_PREC_FP64 */
+    int32_t reserved[7];
+} idw_options;
+
+/* Work counters of the last warp / warpDeriv call. */
+typedef struct idw_stats {
+    int64_t leafPairs;    /* exact (volume node, surface node) pair evaluations */
+    int64_t approx;       /* cluster approximations */
+    int64_t visited;      /* tree nodes whose decision was evaluated */
+    int64_t fp64Fallback; /* mixed mode: decisions re-evaluated in FP64 */
+    int64_t nUnique;      /* unique surface nodes */
+    int64_t nTreeNodes;
+    int64_t maxDepth;
+    int64_t nVol;
+    int64_t nSurfPts;
+    int64_t nLoop;
+    double Ldef0;
+    double lastKernelMs;  /* device time of the last evaluation kernel(s) */
+    int64_t reserved[4];
+} idw_stats;
+
+/* Fill `o` with the reference defaults (idwarp/UnstructuredMesh.py:124-145). */
+void idw_default_options(idw_options *o);
+
+/* Create / destroy a context on the current CUDA device.  (replaces MExt +
+ * initpetsc, idwarp/UnstructuredMesh.py:93-99, libidwarp.pyf:10-12) */
+int idw_create(const idw_options *opts, void **ctx_out);
+int idw_destroy(void *ctx);
+
+/* Copy the last error message (NUL-terminated, truncated to len). */
+int idw_last_error(void *ctx, char *buf, int len);
+
+/* Use `stream` (a cudaStream_t, NULL = default stream) for all later work. */
+int idw_set_stream(void *ctx, void *stream);
+int idw_synchronize(void *ctx);
+
+/* Update options (UnstructuredMesh.py:1051-1069 _setMeshOptions).  As in the
+ * reference, aExp/bExp/bucketSize/cornerAngle/zeroCornerRotations take effect
+ * only at the next idw_initialize_warping; LdefFact, alpha, errTol, evalMode,
+ * useRotations and precision take effect at the next warp. */
+int idw_set_options(void *ctx, const idw_options *opts);
+
+/* Volume grid in common (file) order.  (createcommongrid, libidwarp.pyf:14-17,
+ * src/IO/createGrid.F90) */
+int idw_create_common_grid(void *ctx, const double *volnodes, int64_t nvol, int where);
+
+/* Symmetry planes, at most 6.  (setsymmetryplanes, libidwarp.pyf:69-73,
+ * src/warp/initializeWarping.F90:511-531) */
+int idw_set_symmetry_planes(void *ctx, const double *pts, const double *normals, int32_t n);
+
+/* Merge surface points within tol (squared distance <= tol^2).  uniquepts
+ * (n,3) and link (n, 1-based) are caller-allocated.  (pointreduce,
+ * libidwarp.pyf:195-202, src/utils/pointReduce.F90:1-83) */
+int idw_point_reduce(const double *pts, int32_t n, double tol, double *uniquepts, int32_t *link,
+                     int32_t *nunique);
+
+/* Build the surface tree, nodal-property state, error tables and the
+ * denominator estimate.  pts are this process's surface points (n,3, caller
+ * order with duplicates); uniquepts are the lexsorted unique points, link maps
+ * every point to its unique point (1-based).  faceConn is 0-based into pts.
+ * (initializewarping, libidwarp.pyf:55-67, src/warp/initializeWarping.F90:1-247,
+ * src/modules/kd_tree.F90:1365-1545) */
+int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const double *uniquepts, int32_t nunique,
+                           const int32_t *link, const int32_t *faceSizes, int32_t nfaces,
+                           const int32_t *faceConn, int32_t nconn);
+
+/* Surface coordinates (cdof = 3*npts).  (setsurfacecoordinates /
+ * getsurfacecoordinates, libidwarp.pyf:78-86) */
+int idw_set_surface_coordinates(void *ctx, const double *coords, int64_t cdof, int where);
+int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int where);
+
+/* Warp the volume mesh to the current surface.  (warpmesh, libidwarp.pyf:75,
+ * src/warp/warpMesh.F90:1-82) */
+int idw_warp_mesh(void *ctx);
+
+/* Warp nbatch surfaces in one launch sharing the tree walk: coords holds
+ * nbatch stacked (npts,3) surfaces, out receives nbatch stacked (nvol,3)
+ * grids.  The context's stored surface/grid are left unchanged. */
+int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double *out, int where);
+
+/* Current volume grid in warp order (== common order on one GPU).
+ * (getvolumecoordinates, libidwarp.pyf:45-48; getcommonvolumecoordinates
+ * :50-53) */
+int idw_get_volume_coordinates(void *ctx, double *out, int64_t ndof, int where);
+int idw_get_common_volume_coordinates(void *ctx, double *out, int64_t ndof, int where);
+/* (setvolumecoordinates, src/warp/getVolumeCoordinates.F90:25-46) */
+int idw_set_volume_coordinates(void *ctx, const double *in, int64_t ndof, int where);
+
+/* Solver ordering: ind are 0-based DOF indices into the common grid.
+ * (setexternalmeshindices, libidwarp.pyf:40-43, src/warp/setExternalMeshIndices.F90)
+ * warp->solver is a gather; solver->warp is a scatter-add
+ * (src/warp/gridTransform.F90:4-99). */
+int idw_set_external_mesh_indices(void *ctx, const int32_t *ind, int64_t ndof_solver);
+int idw_get_solver_mesh_dof(void *ctx, int64_t *ndof);
+int idw_warp_to_solver_grid(void *ctx, const double *warp, int64_t wdof, double *solver, int64_t sdof, int where);
+int idw_solver_to_warp_grid(void *ctx, const double *solver, int64_t sdof, double *warp, int64_t wdof, int where);
+
+/* Reverse derivative dXs = (dXv/dXs)^T dXv using the denominator of the last
+ * idw_warp_mesh; fetch the result with idw_get_dxs.  (warpderiv,
+ * libidwarp.pyf:102-105, src/warp/warpDeriv.F90:1-131; getdxs :114-117) */
+int idw_warp_deriv(void *ctx, const double *dxv, int64_t ndof, int where);
+int idw_get_dxs(void *ctx, double *out, int64_t ndof, int where);
+
+/* nseeds reverse derivatives in one launch sharing the tree walk: dxv holds
+ * nseeds stacked (nvol,3) seeds, dxs receives nseeds stacked (npts,3). */
+int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *dxs, int where);
+
+/* Denominator estimate denominator0 (nvol), in common order.
+ * (initializeWarping.F90:241-247) */
+int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where);
+
+/* Counters of the last call. */
+int idw_get_stats(void *ctx, idw_stats *out);
+
+/* Tree / nodal-property state for inspection (tree order, preorder nodes).
+ * nodeInfo: 4 ints per node (l, u, escape, isLeaf); nodeGeom: 4 doubles per
+ * node (X, oradius); nodeErr: 12 per node; nodeAi: 1 per node.
+ * Surface: Xu0 (3), Ai, normals0 (3), isCorner, XuInd per unique node. */
+int idw_get_tree(void *ctx, int32_t *nodeInfo, double *nodeGeom, double *nodeErr, double *nodeAi);
+int idw_get_surface_state(void *ctx, double *xu0, double *ai, double *normals0, int32_t *isCorner,
+                          int32_t *xuInd);
+/* Per-unique-node rotation Mi (9, row-major) and translation Bi (3) of the
+ * current surface (computeNodalProperties, kd_tree.F90:1580-1664). */
+int idw_get_nodal_properties(void *ctx, double *mi, double *bi);
+
+/* Diagnostic: measured FP32 FFMA throughput of the current device (TFLOP/s),
+ * the denominator of the mixed walk's roofline.  No reference counterpart. */
+int idw_probe_ffma(void *stream, int device, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IDWARP_GB300_H */

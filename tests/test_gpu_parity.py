@@ -1,0 +1,238 @@
+"""GPU parity: the CUDA library through its C ABI against the oracle.
+
+Integer/index state (tree, permutation, counts) must match exactly; floating
+point results within the tolerances written in each test.  FP64 GPU vs FP64
+oracle differs only by operation order/FMA contraction and by integer powers
+computed by multiplication instead of pow(), so the bar is ~1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+from tests.meshes import build_gpu, build_oracle, sphere_small, wing_small
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12  # max |GPU - oracle| / Ldef for the FP64 form
+
+
+@pytest.fixture(scope="module")
+def sphere():
+    return sphere_small()
+
+
+@pytest.fixture(scope="module")
+def wing():
+    return wing_small()
+
+
+def _ldef(om):
+    return om.ldef0()
+
+
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_tree_matches_oracle(case, sphere, wing, built_lib, oracle_lib):
+    m = sphere if case == "sphere" else wing
+    om = build_oracle(m)
+    g = build_gpu(m)
+    to, tg = om.tree(), g.getTree()
+    np.testing.assert_array_equal(to["l"], tg["l"])
+    np.testing.assert_array_equal(to["u"], tg["u"])
+    np.testing.assert_array_equal(to["escape"], tg["escape"])
+    np.testing.assert_array_equal(to["dnum"] == 0, tg["isLeaf"] == 1)
+    np.testing.assert_allclose(tg["X"], to["X"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(tg["oradius"], to["oradius"], rtol=1e-13)
+    np.testing.assert_allclose(tg["Ai"], to["Ai"], rtol=1e-12)
+    interior = to["dnum"] != 0
+    # err_j = RMS(dExact - dApprox): at large radii dExact and dApprox agree to
+    # many digits, so the summation order (chunked on the GPU) moves err by
+    # ~1e-16 of dExact; dExact itself is bounded by the innermost error here.
+    eo, eg = to["err"][interior], tg["err"][interior]
+    scale = np.maximum(eo[:, :1], 1e-300)
+    assert np.all(np.abs(eg - eo) <= 1e-10 * scale + 1e-9 * np.abs(eo)), np.max(np.abs(eg - eo) / scale)
+    so, sg = om.surface(), g.getSurfaceState()
+    np.testing.assert_array_equal(so["Xu0"], sg["Xu0"])
+    np.testing.assert_array_equal(so["XuInd"], sg["XuInd"])
+    np.testing.assert_array_equal(so["isCorner"], sg["isCorner"])
+    np.testing.assert_allclose(sg["Ai"], so["Ai"], rtol=1e-12)
+    np.testing.assert_allclose(sg["normals0"], so["normals0"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(g.getDenominator0(), om.den0(), rtol=1e-12)
+
+
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_nodal_properties_match_oracle(case, sphere, wing, built_lib, oracle_lib):
+    m = sphere if case == "sphere" else wing
+    om = build_oracle(m)
+    g = build_gpu(m)
+    om.set_surface_coordinates(m["xs"])
+    g.setSurfaceCoordinates(m["xs"])
+    Mo, Bo = om.nodal()
+    Mg, Bg = g.getNodalProperties()
+    np.testing.assert_allclose(Mg, Mo, atol=1e-13)
+    np.testing.assert_allclose(Bg, Bo, atol=1e-12)
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_warp_fp64_matches_oracle(case, mode, sphere, wing, built_lib, oracle_lib):
+    m = sphere if case == "sphere" else wing
+    om = build_oracle(m, {"evalMode": mode})
+    g = build_gpu(m, {"evalMode": mode}, precision="fp64")
+    om.set_surface_coordinates(m["xs"])
+    g.setSurfaceCoordinates(m["xs"])
+    xo = om.warp()
+    g.warpMesh()
+    xg = g.getWarpGrid().reshape(-1, 3)
+    L = _ldef(om)
+    assert np.abs(xg - xo).max() / L < TOL_FP64
+    so, sg = om.stats(), g.getStats()
+    # identical decisions -> identical work counts
+    assert sg["leafPairs"] == so["leafPairs"]
+    assert sg["approx"] == so["approx"]
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_warp_deriv_fp64_matches_oracle(case, mode, sphere, wing, built_lib, oracle_lib):
+    m = sphere if case == "sphere" else wing
+    om = build_oracle(m, {"evalMode": mode})
+    g = build_gpu(m, {"evalMode": mode}, precision="fp64")
+    om.set_surface_coordinates(m["xs"])
+    g.setSurfaceCoordinates(m["xs"])
+    om.warp()
+    g.warpMesh()
+    rng = np.random.default_rng(1)
+    dxv = rng.normal(size=m["xv0"].shape)
+    do = om.warp_deriv(dxv)
+    g.warpDeriv(dxv.ravel(), solverVec=False)
+    dg = g.getdXs()
+    scale = np.abs(do).max()
+    assert np.abs(dg - do).max() <= 1e-10 * scale
+
+
+def test_warp_deriv_batch_matches_single(wing, built_lib):
+    g = build_gpu(wing, precision="fp64")
+    g.setSurfaceCoordinates(wing["xs"])
+    g.warpMesh()
+    rng = np.random.default_rng(4)
+    seeds = rng.normal(size=(5,) + wing["xv0"].shape)
+    batch = g.warpDerivBatch(seeds)
+    for s in range(5):
+        g.warpDeriv(seeds[s].ravel(), solverVec=False)
+        single = g.getdXs()
+        np.testing.assert_allclose(batch[s], single, rtol=1e-12, atol=1e-12 * np.abs(single).max())
+
+
+def test_rigid_translation_gpu(sphere, built_lib):
+    g = build_gpu(sphere, precision="fp64")
+    t = np.array([0.25, 0.5, -0.125])
+    g.setSurfaceCoordinates(sphere["pts"] + t)
+    g.warpMesh()
+    xv = g.getWarpGrid().reshape(-1, 3)
+    np.testing.assert_allclose(xv - sphere["xv0"], np.broadcast_to(t, xv.shape), atol=1e-12)
+
+
+def test_options_take_effect_like_reference(wing, built_lib, oracle_lib):
+    # LdefFact, alpha, useRotations act at the next warp; errTol too.
+    opts = {"LdefFact": 2.0, "alpha": 0.5, "useRotations": False, "errTol": 5e-4}
+    om = build_oracle(wing, opts)
+    g = build_gpu(wing, opts, precision="fp64")
+    om.set_surface_coordinates(wing["xs"])
+    g.setSurfaceCoordinates(wing["xs"])
+    xo = om.warp()
+    g.warpMesh()
+    assert np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / om.ldef0() < TOL_FP64
+
+
+def test_solver_ordering_roundtrip(wing, built_lib):
+    g = build_gpu(wing, precision="fp64")
+    n = 3 * len(wing["xv0"])
+    rng = np.random.default_rng(8)
+    ind = rng.permutation(n)[: n // 2]
+    g.setExternalMeshIndices(ind)
+    g.setSurfaceCoordinates(wing["xs"])
+    g.warpMesh()
+    np.testing.assert_array_equal(g.getSolverGrid(), g.getWarpGrid()[ind])
+    # the reverse of a gather is a scatter-add
+    v = rng.normal(size=len(ind))
+    w = g._solverToWarp(v)
+    ref = np.zeros(n)
+    np.add.at(ref, ind, v)
+    np.testing.assert_allclose(w, ref, atol=0)
+
+
+def test_errors_are_raised(sphere, built_lib):
+    from idwarp_gb300 import Error
+    from idwarp_gb300._lib import LibraryError
+
+    g = build_gpu(sphere, precision="fp64")
+    with pytest.raises(Error):
+        g.setSurfaceCoordinates(sphere["pts"][:-1])
+    bad = sphere["pts"].copy()
+    bad[3, 1] = np.nan
+    with pytest.raises(Error):
+        g.setSurfaceCoordinates(bad)
+    with pytest.raises(LibraryError):
+        g.warpDeriv(np.zeros(3 * len(sphere["xv0"])), solverVec=False)  # before warpMesh
+
+
+TOL_MIXED = 1e-8  # max |mixed - FP64| / Ldef (precision error on the same tree and decisions)
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_mixed_matches_fp64_same_decisions(case, mode, sphere, wing, built_lib):
+    m = sphere if case == "sphere" else wing
+    g64 = build_gpu(m, {"evalMode": mode}, precision="fp64")
+    g32 = build_gpu(m, {"evalMode": mode}, precision="mixed")
+    for g in (g64, g32):
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+    x64 = g64.getWarpGrid().reshape(-1, 3)
+    x32 = g32.getWarpGrid().reshape(-1, 3)
+    s64, s32 = g64.getStats(), g32.getStats()
+    assert s32["leafPairs"] == s64["leafPairs"]
+    assert s32["approx"] == s64["approx"]
+    err = np.abs(x32 - x64).max() / s64["Ldef0"]
+    assert err < TOL_MIXED, err
+
+
+def test_mixed_matches_oracle_fast(wing, built_lib, oracle_lib):
+    om = build_oracle(wing)
+    g = build_gpu(wing, precision="mixed")
+    om.set_surface_coordinates(wing["xs"])
+    g.setSurfaceCoordinates(wing["xs"])
+    xo = om.warp()
+    g.warpMesh()
+    err = np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / om.ldef0()
+    assert err < TOL_MIXED, err
+
+
+def test_mixed_general_exponents(sphere, built_lib, oracle_lib):
+    # non-(3,5) integer exponents and real exponents take the other weight paths
+    for a, b in ((4.0, 6.0), (2.5, 4.5)):
+        opts = {"aExp": a, "bExp": b}
+        om = build_oracle(sphere, opts)
+        g64 = build_gpu(sphere, opts, precision="fp64")
+        g32 = build_gpu(sphere, opts, precision="mixed")
+        om.set_surface_coordinates(sphere["xs"])
+        xo = om.warp()
+        for g, tol in ((g64, TOL_FP64), (g32, 1e-7)):
+            g.setSurfaceCoordinates(sphere["xs"])
+            g.warpMesh()
+            err = np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / om.ldef0()
+            assert err < tol, (a, b, err)
+
+
+def test_mixed_denominator_feeds_deriv(wing, built_lib, oracle_lib):
+    # warpDeriv after a mixed warpMesh uses the mixed run's (unscaled) denominator
+    om = build_oracle(wing)
+    g = build_gpu(wing, precision="mixed")
+    om.set_surface_coordinates(wing["xs"])
+    g.setSurfaceCoordinates(wing["xs"])
+    om.warp()
+    g.warpMesh()
+    rng = np.random.default_rng(2)
+    dxv = rng.normal(size=wing["xv0"].shape)
+    do = om.warp_deriv(dxv)
+    g.warpDeriv(dxv.ravel(), solverVec=False)
+    assert np.abs(g.getdXs() - do).max() <= 1e-7 * np.abs(do).max()
