@@ -99,6 +99,7 @@ class USMesh(BaseSolver):
             "restartFile": [(str, type(None)), None],
             "bucketSize": [int, 8],
             "precision": [str, ["mixed", "fp64"]],
+            "mixedGate": [float, 3e-3],
         }
 
     # ------------------------------------------------------------------
@@ -343,6 +344,13 @@ class USMesh(BaseSolver):
                     "getDenominator0")
         return out
 
+    def getDenominator(self):
+        """sum(w) per volume node from the last warpMesh (used by warpDeriv)."""
+        out = np.zeros(self.nVol)
+        self._chk(self.lib.idw_get_denominator(self.ctx, C.c_void_p(out.ctypes.data), self.nVol, _lib.IDW_HOST),
+                  "getDenominator")
+        return out
+
     def getTree(self):
         """Tree arrays (preorder nodes): l, u, escape, isLeaf, X, oradius, err (12), Ai."""
         nn = self.getStats()["nTreeNodes"]
@@ -443,6 +451,7 @@ class USMesh(BaseSolver):
         o.bucketSize = self.getOption("bucketSize")
         o.evalMode = _lib.IDW_EVAL_FAST if self.getOption("evalMode") == "fast" else _lib.IDW_EVAL_EXACT
         o.precision = _lib.IDW_PREC_MIXED if self.getOption("precision") == "mixed" else _lib.IDW_PREC_FP64
+        o.mixedGate = self.getOption("mixedGate")
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

@@ -28,7 +28,8 @@ class idw_options(C.Structure):
         ("aExp", C.c_double), ("bExp", C.c_double), ("LdefFact", C.c_double), ("alpha", C.c_double),
         ("errTol", C.c_double), ("symmTol", C.c_double), ("cornerAngle", C.c_double),
         ("evalMode", C.c_int32), ("useRotations", C.c_int32), ("zeroCornerRotations", C.c_int32),
-        ("bucketSize", C.c_int32), ("precision", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("bucketSize", C.c_int32), ("precision", C.c_int32), ("diagnostics", C.c_int32),
+        ("mixedGate", C.c_double), ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -37,7 +38,8 @@ class idw_stats(C.Structure):
         ("leafPairs", C.c_int64), ("approx", C.c_int64), ("visited", C.c_int64), ("fp64Fallback", C.c_int64),
         ("nUnique", C.c_int64), ("nTreeNodes", C.c_int64), ("maxDepth", C.c_int64), ("nVol", C.c_int64),
         ("nSurfPts", C.c_int64), ("nLoop", C.c_int64), ("Ldef0", C.c_double), ("lastKernelMs", C.c_double),
-        ("reserved", C.c_int64 * 4),
+        ("warpLeafSlots", C.c_int64), ("warpNodeSlots", C.c_int64), ("preciseTerms", C.c_int64),
+        ("reserved", C.c_int64 * 1),
     ]
 
     def as_dict(self):
@@ -81,6 +83,7 @@ _SIGS = {
     "idw_get_dxs": [_VP, _VP, C.c_int64, C.c_int],
     "idw_warp_deriv_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_get_denominator0": [_VP, _VP, C.c_int64, C.c_int],
+    "idw_get_denominator": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_stats": [_VP, C.POINTER(idw_stats)],
     "idw_get_tree": [_VP, _IP, _DP, _DP, _DP],
     "idw_get_surface_state": [_VP, _DP, _DP, _DP, _IP, _IP],

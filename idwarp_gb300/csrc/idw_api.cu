@@ -67,8 +67,9 @@ struct Ctx {
     DevBuf<double> nodeErr, nodeAi, nodeMB;
     bool haveTree = false, haveWarp = false, nodalValid = false;
     // FP32 companion arrays of the mixed-precision walk
-    DevBuf<float4> cHi, cLo, ptDA;
-    DevBuf<float> errF, ptDM, nodeDC;
+    DevBuf<float4> cHi, cLo, ptDA, ptDL;
+    DevBuf<float4> recHi, recLo, acc;  // per-volume-node walk records and accumulators
+    DevBuf<float> errF, ptDM, ptDMl, nodeDC, nodeDCl, nodeALo;
     // adjoint
     DevBuf<double> ptAdj, nodeAdj, xub, dxs;
     bool haveDxs = false;
@@ -189,6 +190,7 @@ int validate_options(Ctx *c, const idw_options *o) {
         return fail(c, IDW_ERR_ARG, "precision must be IDW_PREC_FP64 or IDW_PREC_MIXED");
     if (o->bucketSize < 1) return fail(c, IDW_ERR_ARG, "bucketSize must be >= 1");
     if (!(o->LdefFact > 0.0)) return fail(c, IDW_ERR_ARG, "LdefFact must be > 0");
+    if (!(o->mixedGate >= 0.0)) return fail(c, IDW_ERR_ARG, "mixedGate must be >= 0");
     return IDW_OK;
 }
 
@@ -200,8 +202,8 @@ int refresh_nodal(Ctx *c) {
                  c->stream);
     launch_set_data(tree_dev(c), c->ptMB.p, c->nodeMB.p, c->stream);
     if (c->opt.precision == IDW_PREC_MIXED) {
-        launch_mixed_nodal(c->nUnique, c->ptXA.p, c->ptMB.p, c->ptDM.p, c->stream);
-        launch_mixed_nodes(tree_dev(c), c->nodeMB.p, c->nodeDC.p, c->stream);
+        launch_mixed_nodal(c->nUnique, c->ptXA.p, c->ptMB.p, c->ptDM.p, c->ptDMl.p, c->stream);
+        launch_mixed_nodes(tree_dev(c), c->nodeMB.p, c->nodeDC.p, c->nodeDCl.p, c->stream);
     }
     c->nodalValid = true;
     return check_launch(c, "nodal properties");
@@ -231,6 +233,8 @@ void idw_default_options(idw_options *o) {
     o->zeroCornerRotations = 1;
     o->bucketSize = 8;
     o->precision = IDW_PREC_MIXED;
+    o->diagnostics = 0;
+    o->mixedGate = 3e-3;
 }
 
 int idw_create(const idw_options *opts, void **ctx_out) {
@@ -257,7 +261,7 @@ int idw_create(const idw_options *opts, void **ctx_out) {
     }
     c->sym.n = 0;
     c->sym.nLoop = 1;
-    if (c->counters.alloc(4) != cudaSuccess) {
+    if (c->counters.alloc(8) != cudaSuccess) {
         delete c;
         return IDW_ERR_NOMEM;
     }
@@ -468,8 +472,12 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->cLo.alloc(nn));
     CKA(c->errF.alloc(kNerr * size_t(nn)));
     CKA(c->nodeDC.alloc(12 * size_t(nn)));
+    CKA(c->nodeDCl.alloc(12 * size_t(nn)));
+    CKA(c->nodeALo.alloc(nn));
     CKA(c->ptDA.alloc(n));
+    CKA(c->ptDL.alloc(n));
     CKA(c->ptDM.alloc(12 * size_t(n)));
+    CKA(c->ptDMl.alloc(12 * size_t(n)));
     cudaStream_t st = c->stream;
     CK(cudaMemcpyAsync(c->xs.p, pts, 3 * sizeof(double) * npts, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->xuInd.p, xuInd.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
@@ -518,7 +526,8 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     if (e) return e;
     // FP32 companions: split centroids, radii, areas, error tables, leaf offsets
     {
-        std::vector<float4> hi(nn), lo(nn), da(n);
+        std::vector<float4> hi(nn), lo(nn), da(n), dl(n);
+        std::vector<float> alo(nn);
         for (int k = 0; k < nn; ++k) {
             float h[3], l[3];
             for (int q = 0; q < 3; ++q) {
@@ -527,21 +536,37 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
             }
             hi[k] = make_float4(h[0], h[1], h[2], float(t.oradius[k]));
             lo[k] = make_float4(l[0], l[1], l[2], float(nodeAi[k]));
+            alo[k] = float(nodeAi[k] - double(float(nodeAi[k])));
             if (t.leaf[k]) {
-                for (int i = t.l[k]; i <= t.u[k]; ++i)
-                    da[i] = make_float4(float(xa[i].x - t.X[3 * k]), float(xa[i].y - t.X[3 * k + 1]),
-                                        float(xa[i].z - t.X[3 * k + 2]), float(ai[i]));
+                for (int i = t.l[k]; i <= t.u[k]; ++i) {
+                    const double d[3] = {xa[i].x - t.X[3 * k], xa[i].y - t.X[3 * k + 1], xa[i].z - t.X[3 * k + 2]};
+                    float dh[3], dlo[3];
+                    for (int q = 0; q < 3; ++q) {
+                        dh[q] = float(d[q]);
+                        dlo[q] = float(d[q] - double(dh[q]));
+                    }
+                    da[i] = make_float4(dh[0], dh[1], dh[2], float(ai[i]));
+                    dl[i] = make_float4(dlo[0], dlo[1], dlo[2], float(ai[i] - double(float(ai[i]))));
+                }
             }
         }
         CK(cudaMemcpyAsync(c->cHi.p, hi.data(), sizeof(float4) * nn, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(c->cLo.p, lo.data(), sizeof(float4) * nn, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(c->ptDA.p, da.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->ptDL.p, dl.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->nodeALo.p, alo.data(), sizeof(float) * nn, cudaMemcpyHostToDevice, st));
         launch_to_float(int64_t(kNerr) * nn, c->nodeErr.p, c->errF.p, st);
         CK(cudaStreamSynchronize(st));
     }
     // denominator estimate over the mirrors (initializeWarping.F90:241-247)
     launch_denominator0(tree_dev(c), c->ptXA.p, vol_dev(c), law0, c->sym, c->den0.p, st);
     e = check_launch(c, "denominator0");
+    if (e) return e;
+    CKA(c->recHi.alloc(size_t(c->sym.nLoop) * c->nVol));
+    CKA(c->recLo.alloc(size_t(c->sym.nLoop) * c->nVol));
+    CKA(c->acc.alloc(2 * size_t(c->nVol)));
+    launch_walk_records(vol_dev(c), c->sym, c->optInit.bExp, c->recHi.p, c->recLo.p, st);
+    e = check_launch(c, "walk records");
     if (e) return e;
     CK(cudaStreamSynchronize(st));
     c->haveTree = true;
@@ -588,6 +613,9 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     k.law = make_law(c);
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
+    k.slotStats = c->opt.diagnostics & 1;
+    // terms whose weight share x lever arm exceeds mixedGate*Ldef are summed in double-float
+    k.precGate = c->opt.mixedGate * c->Ldef0 * c->opt.LdefFact;
     PointsDev p;
     p.xa = c->ptXA.p;
     p.mb = c->ptMB.p;
@@ -595,20 +623,27 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     o.xv = xvOut;
     o.den = denOut;
     o.counters = c->counters.p;
-    CK(cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     if (c->opt.precision == IDW_PREC_MIXED) {
         TreeDevF tf;
         tf.cHi = c->cHi.p;
         tf.cLo = c->cLo.p;
+        tf.aLo = c->nodeALo.p;
         tf.err = c->errF.p;
         PointsDevF pf;
         pf.da = c->ptDA.p;
+        pf.dl = c->ptDL.p;
         pf.dm = c->ptDM.p;
+        pf.dml = c->ptDMl.p;
         NodeAggF af;
         af.dc = c->nodeDC.p;
-        launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), k, exact, o, c->stream);
+        af.dcl = c->nodeDCl.p;
+        WalkRecF rec;
+        rec.hi = c->recHi.p;
+        rec.lo = c->recLo.p;
+        launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), rec, k, exact, c->acc.p, o, c->stream);
     } else {
         launch_walk_fp64(tree_dev(c), p, vol_dev(c), c->nodeMB.p, k, exact, c->nUnique, o, c->stream);
     }
@@ -618,13 +653,16 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
 }
 
 static int read_counters(Ctx *c) {
-    unsigned long long h[4];
+    unsigned long long h[8];
     CK(cudaMemcpyAsync(h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    c->stats.warpLeafSlots = int64_t(h[4]);
+    c->stats.warpNodeSlots = int64_t(h[5]);
     CK(cudaStreamSynchronize(c->stream));
     c->stats.leafPairs = int64_t(h[0]);
     c->stats.approx = int64_t(h[1]);
     c->stats.visited = int64_t(h[2]);
     c->stats.fp64Fallback = int64_t(h[3]);
+    c->stats.preciseTerms = int64_t(h[6]);
     if (c->eventsRecorded) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->stats.lastKernelMs = ms;
@@ -714,6 +752,15 @@ int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where) {
     return copy_out(c, out, c->den0.p, size_t(nvol), where);
 }
 
+int idw_get_denominator(void *ctx, double *out, int64_t nvol, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh has not been called");
+    if (nvol != c->nVol) return fail(c, IDW_ERR_ARG, "nvol mismatch");
+    CK(cudaSetDevice(c->device));
+    return copy_out(c, out, c->den.p, size_t(nvol), where);
+}
+
 static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStride, double *dxsOut, int where,
                      int64_t dxsStride) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
@@ -724,6 +771,8 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     k.law = make_law(c);
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
+    k.slotStats = 0;
+    k.precGate = 0.0;
     PointsDev p;
     p.xa = c->ptXA.p;
     p.mb = c->ptMB.p;
@@ -734,7 +783,7 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     CKA(nodeAdj.alloc(size_t(nSeeds) * 12 * nn));
     CK(cudaMemsetAsync(ptAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * n, c->stream));
     CK(cudaMemsetAsync(nodeAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * nn, c->stream));
-    CK(cudaMemsetAsync(c->counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
     launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride, ptAdj.p,
                              nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);

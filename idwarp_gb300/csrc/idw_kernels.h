@@ -28,7 +28,8 @@ struct TreeDev {
 // FP32 companion arrays of the mixed-precision path (set-up constants).
 struct TreeDevF {
     const float4 *cHi;   // centroid high part, oradius
-    const float4 *cLo;   // centroid low part, node area A
+    const float4 *cLo;   // centroid low part, node area A (high part)
+    const float *aLo;    // node area A, low part
     const float *err;    // 12 per node (true weight units)
 };
 
@@ -39,12 +40,32 @@ struct PointsDev {
 };
 
 struct PointsDevF {
-    const float4 *da;    // Xu0 - centroid(leaf), Ai  (FP32, set-up constant)
-    const float *dm;     // 12 per point: D = M - I (9), u = M Xu0 + b - Xu0 (3)
+    const float4 *da;    // Xu0 - centroid(leaf) high part, Ai  (FP32, set-up constant)
+    const float4 *dl;    // Xu0 - centroid(leaf) low part, Ai low part
+    const float *dm;     // 12 per point: D = M - I (9), u = M Xu0 + b - Xu0 (3), high parts
+    const float *dml;    // the same, low parts
+};
+
+// Per volume node (Morton order) and mirror: FP32 walk records.
+struct WalkRecF {
+    const float4 *hi;  // mirrored point, high part; denominator estimate (FP32)
+    const float4 *lo;  // mirrored point, low part; scale exponent s (int bits)
+};
+
+struct MixedParams {
+    int nLoop, nSym;
+    float nrm[kMaxSym][3], nrmLo[kMaxSym][3];
+    float LdefF, alphaToBexpF, errTolF;
+    double errTol;
+    int intExp, dExp;
+    float dExpF;
+    int slotStats;  // count warp-level lane slots (diagnostics)
+    float LdefLo, abH, abL, precGate;
 };
 
 struct NodeAggF {
-    const float *dc;     // 12 per node: Dbar = Mbar - I (9), c = Mbar X + bbar - X (3)
+    const float *dc;     // 12 per node: Dbar = Mbar - I (9), c = Mbar X + bbar - X (3), high parts
+    const float *dcl;    // the same, low parts
 };
 
 struct VolumeDev {
@@ -64,6 +85,8 @@ struct EvalConsts {
     WeightLaw law;
     double errTol;
     SymPlanes sym;
+    int slotStats;
+    double precGate;  // mixed walk: weight x lever-arm threshold for double-float cluster terms
 };
 
 // Nodal properties (idw_nodal.cu)
@@ -88,14 +111,17 @@ void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, cons
                          unsigned long long *codes, int *idx, cudaStream_t st);
 void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, const double *nodeX,
                          float4 *ptDA, cudaStream_t st);
-void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, cudaStream_t st);
-void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, cudaStream_t st);
+void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, float *ptDMl, cudaStream_t st);
+void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, float *nodeDCl, cudaStream_t st);
 
 // Evaluation (idw_walk.cu)
 void launch_walk_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const double *nodeMB,
                       const EvalConsts &k, int exact, int nPts, const WalkOut &o, cudaStream_t st);
+void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, float4 *hi, float4 *lo,
+                         cudaStream_t st);
 void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
-                       const VolumeDev &v, const EvalConsts &k, int exact, const WalkOut &o, cudaStream_t st);
+                       const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
+                       const WalkOut &o, cudaStream_t st);
 void launch_to_float(int64_t n, const double *src, float *dst, cudaStream_t st);
 int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,
                              int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,

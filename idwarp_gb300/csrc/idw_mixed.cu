@@ -11,8 +11,8 @@
 //   * weights are scaled by sigma^b with sigma = 2^s chosen per volume node
 //     from its denominator estimate, so (L/d)^b stays in FP32 range (the ratio
 //     num/den is unchanged; powers of two scale exactly);
-//   * each leaf's partial sums are added to Kahan-compensated FP32 running
-//     sums; normalisation, mirror reflection and the add-back to Xv0 are FP64.
+//   * each leaf's partial sums are added to compensated (two-sum) FP32 running
+//     sums; normalisation and the add-back to Xv0 are FP64.
 // Open/approximate decisions are taken in FP32 only when they are further
 // from the threshold than the FP32 error bound; otherwise they are re-taken
 // with the FP64 decision of the FP64 form (decide64), so the mixed walk makes
@@ -25,7 +25,7 @@ namespace idw {
 namespace {
 
 struct MixedCounters {
-    unsigned long long leafPairs = 0, approx = 0, visited = 0, fallback = 0;
+    unsigned long long leafPairs = 0, approx = 0, visited = 0, fallback = 0, leafSlots = 0, nodeSlots = 0, precise = 0;
     __device__ void flush(unsigned long long *dst) {
         if (!dst) return;
         unsigned long long a = warp_sum(leafPairs), b = warp_sum(approx), c = warp_sum(visited),
@@ -35,6 +35,12 @@ struct MixedCounters {
             if (b) atomicAdd(dst + 1, b);
             if (c) atomicAdd(dst + 2, c);
             if (d) atomicAdd(dst + 3, d);
+            if (leafSlots) atomicAdd(dst + 4, leafSlots);
+            if (nodeSlots) atomicAdd(dst + 5, nodeSlots);
+        }
+        unsigned long long e = warp_sum(precise);
+        if ((threadIdx.x & 31) == 0) {
+            if (e) atomicAdd(dst + 6, e);
         }
     }
 };
@@ -44,102 +50,199 @@ template <int KIND>
 struct Law32 {
     int ia, ib;
     float fa, fb;
-    __device__ __forceinline__ float eval(float t, float c1, float ab) const {
+    // c1 t^a + (ab + abl) t^b; ab + abl is alpha^b split in two floats so the
+    // FP32 terms carry the same alpha^b as the double-float terms.
+    __device__ __forceinline__ float eval(float t, float c1, float ab, float abl) const {
         if (KIND == 0) {
             float t2 = t * t;
             float t3 = t2 * t;
             float t5 = t3 * t2;
-            return c1 * t3 + ab * t5;
+            return fmaf(c1, t3, fmaf(ab, t5, abl * t5));
         } else if (KIND == 1) {
             float ta = ipowf(t, ia);
             float tb = ta * ipowf(t, ib - ia);
-            return c1 * ta + ab * tb;
+            return fmaf(c1, ta, fmaf(ab, tb, abl * tb));
         } else {
             return c1 * powf(t, fa) + ab * powf(t, fb);
         }
     }
 };
 
+// Compensated summation (Neumaier / Ogita-Rump-Oishi Sum2): the sum is s + c,
+// with every rounding error of the running sum captured exactly by two-sum
+// and collected in c, so the pair is accurate to ~u^2 relative.
 __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
-    float y = x - c;
-    float t = s + y;
-    c = (t - s) - y;
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
     s = t;
 }
 
 __device__ __forceinline__ float4 ldgf4(const float4 *p) { return __ldg(p); }
 
 // FP32 error-table interpolation with a bound on its deviation from the FP64
-// value (see the file comment).  Returns err, sets bnd.
+// value (see the file comment).  dOvrR >= 2 here.  The bracket index follows
+// the radii 2,3,4,5,7.5,10,20,40,...,640: unit steps below 5, then 7.5 and 10,
+// then doublings from 20.  Returns err, sets bnd.
 __device__ __forceinline__ float get_error32(const float *e, float dOvrR, float &bnd) {
-    const float rs[kNerr] = {2.f, 3.f, 4.f, 5.f, 7.5f, 10.f, 20.f, 40.f, 80.f, 160.f, 320.f, 640.f};
-#pragma unroll
-    for (int i = 0; i < kNerr - 1; ++i) {
-        if (dOvrR < rs[i + 1]) {
-            float orst = 1.0f / (rs[i + 1] - rs[i]);
-            float e0 = __ldg(e + i), e1 = __ldg(e + i + 1);
-            float fact = (dOvrR - rs[i]) * orst;
-            bnd = 2e-6f * (dOvrR * orst * fabsf(e1 - e0) + fabsf(e0) + fabsf(e1));
-            return (1.0f - fact) * e0 + fact * e1;
-        }
+    int i;
+    float r0, r1;
+    if (dOvrR < 5.0f) {
+        i = int(dOvrR) - 2;  // 0..2
+        r0 = float(i + 2);
+        r1 = r0 + 1.0f;
+    } else if (dOvrR < 10.0f) {
+        i = dOvrR < 7.5f ? 3 : 4;
+        r0 = i == 3 ? 5.0f : 7.5f;
+        r1 = i == 3 ? 7.5f : 10.0f;
+    } else if (dOvrR < 20.0f) {
+        i = 5;
+        r0 = 10.0f;
+        r1 = 20.0f;
+    } else if (dOvrR < 640.0f) {
+        // 20 * 2^m <= dOvrR < 20 * 2^(m+1), m = 0..4
+        const int m = ((__float_as_int(dOvrR * 0.05f) >> 23) & 0xff) - 127;
+        i = 6 + m;
+        r0 = 20.0f * float(1 << m);
+        r1 = 2.0f * r0;
+    } else {
+        const float e11 = __ldg(e + kNerr - 1);
+        bnd = 2e-6f * fabsf(e11);
+        return e11;
     }
-    float e11 = __ldg(e + kNerr - 1);
-    bnd = 2e-6f * fabsf(e11);
-    return e11;
+    const float orst = 1.0f / (r1 - r0);
+    const float e0 = __ldg(e + i), e1 = __ldg(e + i + 1);
+    const float fact = (dOvrR - r0) * orst;
+    bnd = 2e-6f * (dOvrR * orst * fabsf(e1 - e0) + fabsf(e0) + fabsf(e1));
+    return (1.0f - fact) * e0 + fact * e1;
 }
+
+// Exact difference a - b as (hi, lo) (Knuth two-sum).
+__device__ __forceinline__ void two_diff(float a, float b, float &hi, float &lo) {
+    hi = a - b;
+    const float bb = hi - a;
+    lo = (a - (hi - bb)) - (b + bb);
+}
+
+// ---- double-float (hi + lo) arithmetic for the precision-critical far-field
+// cluster terms (Dekker/Knuth error-free transformations with FMA) ----
+struct dfl {
+    float h, l;
+};
+__device__ __forceinline__ dfl df_norm(float h, float l) {
+    const float s = h + l;
+    return {s, l - (s - h)};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    float s, e;
+    s = a.h + b.h;
+    const float bb = s - a.h;
+    e = (a.h - (s - bb)) + (b.h - bb);
+    e += a.l + b.l;
+    return df_norm(s, e);
+}
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return df_norm(p, e);
+}
+__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
+    const float p = a.h * b;
+    float e = fmaf(a.h, b, -p);
+    e = fmaf(a.l, b, e);
+    return df_norm(p, e);
+}
+// 1/sqrt(q) with one Newton step carried in double-float.
+__device__ __forceinline__ dfl df_rsqrt(dfl q) {
+    const float y0 = rsqrtf(q.h);
+    const float t = y0 * y0;
+    const float te = fmaf(y0, y0, -t);  // y0^2 = t + te exactly
+    const float p = q.h * t;
+    float e = fmaf(q.h, t, -p);
+    e = fmaf(q.h, te, e);
+    e = fmaf(q.l, t, e);
+    const float r = (1.0f - p) - e;  // 1 - q y0^2 (1 - p is exact near 1)
+    return df_norm(y0, 0.5f * y0 * r);
+}
+template <int KIND>
+__device__ __forceinline__ dfl df_pow_int(dfl t, int n) {
+    if (KIND == 0 && n == 3) return df_mul(df_mul(t, t), t);
+    dfl r = {1.0f, 0.0f}, b = t;
+    while (n > 0) {
+        if (n & 1) r = df_mul(r, b);
+        n >>= 1;
+        if (n) b = df_mul(b, b);
+    }
+    return r;
+}
+// Compensated accumulation of a double-float term into a pair (s + c).
+__device__ __forceinline__ void kahan_add_df(float &s, float &c, dfl x) {
+    kahan_add(s, c, x.h);
+    kahan_add(s, c, x.l);
+}
+
+// Power of two 2^e as a float (|e| <= 126).
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + max(-126, min(127, e))) << 23); }
 
 template <int KIND>
 __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af,
-                                                    VolumeDev v, EvalConsts k, Law32<KIND> law, int exact,
-                                                    WalkOut o) {
+                                                    VolumeDev v, WalkRecF rec, MixedParams mp, Law32<KIND> law,
+                                                    int exact, float4 *acc, unsigned long long *counters) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = gid < v.nVol;
-    const int vi = valid ? v.perm[gid] : 0;
-    const double x0[3] = {v.xv0[3 * vi], v.xv0[3 * vi + 1], v.xv0[3 * vi + 2]};
-    const double den0 = v.den0[vi];
-    const double tolDen = k.errTol * den0;
-    // per-node power-of-two scale: sigma^b ~ 1/den0
-    int s = 0;
-    if (den0 > 0.0 && den0 < 1e300) {
-        int e = ilogb(den0);
-        double sb = -double(e) / k.law.bExp;
-        s = max(-40, min(40, int(rint(sb))));
-    }
-    const float Ls = float(ldexp(k.law.Ldef, s));
-    const float c1 = float(exp2(double(s) * (k.law.bExp - k.law.aExp)));
-    const float ab = float(k.law.alphaToBexp);
-    const float tauf = float(fmin(tolDen, 3.0e38));
-    double numer[3] = {0, 0, 0}, denom = 0.0;
+    const int64_t g = valid ? gid : 0;
+    // per-node scale sigma = 2^s (set-up constant, stored with the record)
+    const float4 r0lo = rec.lo[g];
+    const int s = __float_as_int(r0lo.w);
+    const float den0f = rec.hi[g].w;
+    const float Ls = mp.LdefF * pow2f(s);
+    const float LsLo = mp.LdefLo * pow2f(s);
+    const float c1 = mp.intExp ? pow2f(s * mp.dExp) : exp2f(float(s) * mp.dExpF);
+    const float ab = mp.abH, abl = mp.abL;
+    const float tauf = mp.errTolF * den0f;
+    float SN[3] = {0, 0, 0}, CN[3] = {0, 0, 0}, SD = 0.f, CD = 0.f;
     MixedCounters cnt;
-    for (int kk = 0; kk < k.sym.nLoop; ++kk) {
-        double r[3];
-        mirror_point(k.sym, kk, x0, r);
-        float rh[3], rl[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            rh[c] = float(r[c]);
-            rl[c] = float(r[c] - double(rh[c]));
-        }
+    for (int kk = 0; kk < mp.nLoop; ++kk) {
+        const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
+        const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
         float sn[3] = {0, 0, 0}, cn[3] = {0, 0, 0}, sd = 0.f, cd = 0.f;
         int node = 0, skip = 0;
         while (node < t.nNodes) {
             const int4 inf = t.info[node];
             const bool active = valid && node >= skip;
+            if (mp.slotStats && __any_sync(kFull, active)) {
+                if (inf.w)
+                    cnt.leafSlots += 32ull * (inf.y - inf.x + 1);
+                else
+                    cnt.nodeSlots += 32ull;
+            }
             if (inf.w) {
+                bool leafPrecise = false;
                 if (active) {
                     const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
-                    const float rho0 = (rh[0] - ch.x) + (rl[0] - cl.x);
-                    const float rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
-                    const float rho2 = (rh[2] - ch.z) + (rl[2] - cl.z);
+                    // r - C as hi + lo: exact high parts, so a volume node on a
+                    // surface node resolves d^2 = eps (1e-15) to full precision
+                    float h0, h1, h2, l0, l1, l2;
+                    two_diff(rh[0], ch.x, h0, l0);
+                    two_diff(rh[1], ch.y, h1, l1);
+                    two_diff(rh[2], ch.z, h2, l2);
+                    l0 += rl[0] - cl.x;
+                    l1 += rl[1] - cl.y;
+                    l2 += rl[2] - cl.z;
                     float pn0 = 0.f, pn1 = 0.f, pn2 = 0.f, pd = 0.f;
                     for (int i = inf.x; i <= inf.y; ++i) {
-                        const float4 da = ldgf4(pf.da + i);
+                        const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
                         const float4 *dm = reinterpret_cast<const float4 *>(pf.dm + 12 * i);
                         const float4 m0 = ldgf4(dm), m1 = ldgf4(dm + 1), m2 = ldgf4(dm + 2);
-                        const float dx = rho0 - da.x, dy = rho1 - da.y, dz = rho2 - da.z;
+                        const float dx = (h0 - da.x) + (l0 - dl.x);
+                        const float dy = (h1 - da.y) + (l1 - dl.y);
+                        const float dz = (h2 - da.z) + (l2 - dl.z);
                         const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
-                        const float tt = Ls * rsqrtf(d2);
-                        const float w = da.w * law.eval(tt, c1, ab);
+                        const float r1 = rsqrtf(d2);
+                        const float tt = fmaf(Ls, r1, LsLo * r1);
+                        const float w = da.w * law.eval(tt, c1, ab, abl);
                         // S = D dx + u ; D row-major in m0.xyzw m1.xyzw m2.x, u in m2.yzw
                         const float S0 = fmaf(m0.x, dx, fmaf(m0.y, dy, fmaf(m0.z, dz, m2.y)));
                         const float S1 = fmaf(m0.w, dx, fmaf(m1.x, dy, fmaf(m1.y, dz, m2.z)));
@@ -149,29 +252,78 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                         pn2 = fmaf(w, S2, pn2);
                         pd += w;
                     }
-                    kahan_add(sn[0], cn[0], pn0);
-                    kahan_add(sn[1], cn[1], pn1);
-                    kahan_add(sn[2], cn[2], pn2);
-                    kahan_add(sd, cd, pd);
+                    // a leaf carrying a large weight share at a long lever arm is
+                    // re-summed in double-float (same gate as cluster terms)
+                    leafPrecise = KIND != 2 &&
+                                  fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + 0.1f * pd * sqrtf(h0 * h0 + h1 * h1 + h2 * h2) >
+                                      mp.precGate;
+                    if (!leafPrecise) {
+                        kahan_add(sn[0], cn[0], pn0);
+                        kahan_add(sn[1], cn[1], pn1);
+                        kahan_add(sn[2], cn[2], pn2);
+                        kahan_add(sd, cd, pd);
+                    }
                     cnt.leafPairs += inf.y - inf.x + 1;
                     cnt.visited++;
+                }
+                if (__any_sync(kFull, leafPrecise)) {
+                    if (leafPrecise) {
+                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+                        dfl q0, q1, q2;
+                        two_diff(rh[0], ch.x, q0.h, q0.l);
+                        two_diff(rh[1], ch.y, q1.h, q1.l);
+                        two_diff(rh[2], ch.z, q2.h, q2.l);
+                        q0.l += rl[0] - cl.x;
+                        q1.l += rl[1] - cl.y;
+                        q2.l += rl[2] - cl.z;
+                        for (int i = inf.x; i <= inf.y; ++i) {
+                            const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
+                            dfl x0, x1, x2;
+                            two_diff(q0.h, da.x, x0.h, x0.l);
+                            two_diff(q1.h, da.y, x1.h, x1.l);
+                            two_diff(q2.h, da.z, x2.h, x2.l);
+                            x0 = df_norm(x0.h, x0.l + (q0.l - dl.x));
+                            x1 = df_norm(x1.h, x1.l + (q1.l - dl.y));
+                            x2 = df_norm(x2.h, x2.l + (q2.l - dl.z));
+                            const dfl d2d = df_add(df_add(df_add(df_mul(x0, x0), df_mul(x1, x1)), df_mul(x2, x2)),
+                                                   {1e-15f, 0.f});
+                            const dfl tt = df_mul({Ls, LsLo}, df_rsqrt(d2d));
+                            const dfl ta = df_pow_int<KIND>(tt, law.ia);
+                            const dfl tb = df_mul(ta, df_pow_int<KIND>(tt, law.ib - law.ia));
+                            const dfl lawv = df_add({c1 * ta.h, c1 * ta.l}, df_mul(tb, {mp.abH, mp.abL}));
+                            const dfl w = df_mul(lawv, {da.w, dl.w});
+                            const float *mh = pf.dm + 12 * i, *ml = pf.dml + 12 * i;
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) {
+                                dfl acc = {__ldg(mh + 9 + a), __ldg(ml + 9 + a)};
+                                acc = df_add(acc, df_mul({__ldg(mh + 3 * a), __ldg(ml + 3 * a)}, x0));
+                                acc = df_add(acc, df_mul({__ldg(mh + 3 * a + 1), __ldg(ml + 3 * a + 1)}, x1));
+                                acc = df_add(acc, df_mul({__ldg(mh + 3 * a + 2), __ldg(ml + 3 * a + 2)}, x2));
+                                kahan_add_df(sn[a], cn[a], df_mul(w, acc));
+                            }
+                            kahan_add_df(sd, cd, w);
+                        }
+                        cnt.precise += inf.y - inf.x + 1;
+                    }
                 }
                 node = inf.z;
             } else {
                 bool open = false;
+                int dec = 0;  // 0 open, 1 approximate, 2 undecided in FP32
+                float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
                 if (active) {
                     if (exact) {
-                        open = true;
+                        dec = 0;
                     } else {
                         cnt.visited++;
                         const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
-                        const float rho0 = (rh[0] - ch.x) + (rl[0] - cl.x);
-                        const float rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
-                        const float rho2 = (rh[2] - ch.z) + (rl[2] - cl.z);
-                        const float d2 = fmaf(rho0, rho0, fmaf(rho1, rho1, rho2 * rho2));
-                        const float dist = sqrtf(d2);
-                        const float dOvrR = dist * ch.w;
-                        int dec;  // 0 open, 1 approximate, 2 undecided in FP32
+                        wA = cl.w;
+                        rho0 = (rh[0] - ch.x) + (rl[0] - cl.x);
+                        rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
+                        rho2 = (rh[2] - ch.z) + (rl[2] - cl.z);
+                        d2 = fmaf(rho0, rho0, fmaf(rho1, rho1, rho2 * rho2));
+                        rs = rsqrtf(d2);
+                        const float dOvrR = d2 * rs * ch.w;
                         if (dOvrR < 2.0f * (1.0f - 4e-6f)) {
                             dec = 0;
                         } else if (dOvrR <= 2.0f * (1.0f + 4e-6f)) {
@@ -180,78 +332,204 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                             float bnd;
                             float err = get_error32(tf.err + kNerr * node, dOvrR, bnd);
                             bnd += 1e-6f * tauf;
-                            if (err + bnd < tauf)
-                                dec = 1;
-                            else if (err - bnd > tauf)
-                                dec = 0;
-                            else
-                                dec = 2;
+                            dec = (err + bnd < tauf) ? 1 : ((err - bnd > tauf) ? 0 : 2);
                         }
-                        if (dec == 2) {
-                            double dist64;
-                            dec = decide64(t.geom[node], t.err + kNerr * node, r, tolDen, dist64);
-                            cnt.fallback++;
+                    }
+                }
+                // rare: re-take undecided decisions with the FP64 rule (warp-uniform branch)
+                if (__any_sync(kFull, dec == 2)) {
+                    if (dec == 2) {
+                        const int vi = v.perm[g];
+                        double r[3] = {double(rh[0]) + double(rl[0]), double(rh[1]) + double(rl[1]),
+                                       double(rh[2]) + double(rl[2])};
+                        double dist64;
+                        dec = decide64(t.geom[node], t.err + kNerr * node, r, mp.errTol * v.den0[vi], dist64);
+                        cnt.fallback++;
+                    }
+                }
+                bool precise = false;
+                if (dec == 1) {
+                    const float tt = fmaf(Ls, rs, LsLo * rs);
+                    const float w = wA * law.eval(tt, c1, ab, abl);
+                    const float4 *dc = reinterpret_cast<const float4 *>(af.dc + 12 * node);
+                    const float4 m0 = ldgf4(dc), m1 = ldgf4(dc + 1), m2 = ldgf4(dc + 2);
+                    const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
+                    const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
+                    const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
+                    // A far cluster whose share of the weight times its lever arm
+                    // is large enough for FP32 rounding to show in Xv is
+                    // re-evaluated in double-float below.
+                    precise = KIND != 2 && w * (fabsf(S0) + fabsf(S1) + fabsf(S2) + 0.1f * d2 * rs) > mp.precGate;
+                    if (!precise) {
+                        kahan_add(sn[0], cn[0], w * S0);
+                        kahan_add(sn[1], cn[1], w * S1);
+                        kahan_add(sn[2], cn[2], w * S2);
+                        kahan_add(sd, cd, w);
+                    }
+                    skip = inf.z;
+                    cnt.approx++;
+                } else if (active) {
+                    open = true;
+                }
+                if (__any_sync(kFull, precise)) {
+                    if (precise) {
+                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+                        dfl q0, q1, q2;
+                        two_diff(rh[0], ch.x, q0.h, q0.l);
+                        two_diff(rh[1], ch.y, q1.h, q1.l);
+                        two_diff(rh[2], ch.z, q2.h, q2.l);
+                        q0 = df_norm(q0.h, q0.l + (rl[0] - cl.x));
+                        q1 = df_norm(q1.h, q1.l + (rl[1] - cl.y));
+                        q2 = df_norm(q2.h, q2.l + (rl[2] - cl.z));
+                        const dfl d2d = df_add(df_add(df_mul(q0, q0), df_mul(q1, q1)), df_mul(q2, q2));
+                        const dfl tt = df_mul({Ls, LsLo}, df_rsqrt(d2d));
+                        const dfl ta = df_pow_int<KIND>(tt, law.ia);
+                        const dfl tb = df_mul(ta, df_pow_int<KIND>(tt, law.ib - law.ia));
+                        const dfl lawv = df_add({c1 * ta.h, c1 * ta.l}, df_mul(tb, {mp.abH, mp.abL}));
+                        const dfl w = df_mul(lawv, {cl.w, __ldg(tf.aLo + node)});
+                        const float *dh = af.dc + 12 * node, *dlo = af.dcl + 12 * node;
+                        dfl S[3];
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            dfl acc = {__ldg(dh + 9 + a), __ldg(dlo + 9 + a)};
+                            acc = df_add(acc, df_mul({__ldg(dh + 3 * a), __ldg(dlo + 3 * a)}, q0));
+                            acc = df_add(acc, df_mul({__ldg(dh + 3 * a + 1), __ldg(dlo + 3 * a + 1)}, q1));
+                            acc = df_add(acc, df_mul({__ldg(dh + 3 * a + 2), __ldg(dlo + 3 * a + 2)}, q2));
+                            S[a] = acc;
                         }
-                        if (dec == 1) {
-                            const float tt = Ls * rsqrtf(d2);
-                            const float w = cl.w * law.eval(tt, c1, ab);
-                            const float4 *dc = reinterpret_cast<const float4 *>(af.dc + 12 * node);
-                            const float4 m0 = ldgf4(dc), m1 = ldgf4(dc + 1), m2 = ldgf4(dc + 2);
-                            const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
-                            const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
-                            const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
-                            kahan_add(sn[0], cn[0], w * S0);
-                            kahan_add(sn[1], cn[1], w * S1);
-                            kahan_add(sn[2], cn[2], w * S2);
-                            kahan_add(sd, cd, w);
-                            skip = inf.z;
-                            cnt.approx++;
-                        } else {
-                            open = true;
-                        }
+                        kahan_add_df(sn[0], cn[0], df_mul(w, S[0]));
+                        kahan_add_df(sn[1], cn[1], df_mul(w, S[1]));
+                        kahan_add_df(sn[2], cn[2], df_mul(w, S[2]));
+                        kahan_add_df(sd, cd, w);
+                        cnt.precise++;
                     }
                 }
                 node = __any_sync(kFull, open) ? node + 1 : inf.z;
             }
         }
-        double num[3] = {double(sn[0]) - double(cn[0]), double(sn[1]) - double(cn[1]), double(sn[2]) - double(cn[2])};
-        mirror_vector(k.sym, kk, num);
-        numer[0] += num[0];
-        numer[1] += num[1];
-        numer[2] += num[2];
-        denom += double(sd) - double(cd);
+        // reflect this mirror's numerator back (vector reflection) and
+        // accumulate, all in double-float so no digits are lost between mirrors
+        if (mp.nLoop == 1) {
+            SN[0] = sn[0]; SN[1] = sn[1]; SN[2] = sn[2]; SD = sd;
+            CN[0] = cn[0]; CN[1] = cn[1]; CN[2] = cn[2]; CD = cd;
+        } else {
+            dfl num[3] = {df_norm(sn[0], cn[0]), df_norm(sn[1], cn[1]), df_norm(sn[2], cn[2])};
+#pragma unroll
+            for (int j = 0; j < kMaxSym; ++j) {
+                if (j < mp.nSym && ((kk >> j) & 1)) {
+                    const dfl n0 = {mp.nrm[j][0], mp.nrmLo[j][0]}, n1 = {mp.nrm[j][1], mp.nrmLo[j][1]},
+                              n2 = {mp.nrm[j][2], mp.nrmLo[j][2]};
+                    dfl dp = df_add(df_add(df_mul(num[0], n0), df_mul(num[1], n1)), df_mul(num[2], n2));
+                    dp = {-2.0f * dp.h, -2.0f * dp.l};
+                    num[0] = df_add(num[0], df_mul(dp, n0));
+                    num[1] = df_add(num[1], df_mul(dp, n1));
+                    num[2] = df_add(num[2], df_mul(dp, n2));
+                }
+            }
+            kahan_add_df(SN[0], CN[0], num[0]);
+            kahan_add_df(SN[1], CN[1], num[1]);
+            kahan_add_df(SN[2], CN[2], num[2]);
+            kahan_add_df(SD, CD, df_norm(sd, cd));
+        }
     }
     if (valid) {
-        double oden = 1.0 / denom;
-        if (o.xv) {
-            o.xv[3 * vi + 0] = x0[0] + numer[0] * oden;
-            o.xv[3 * vi + 1] = x0[1] + numer[1] * oden;
-            o.xv[3 * vi + 2] = x0[2] + numer[2] * oden;
-        }
-        // true-unit denominator: divide out sigma^b
-        if (o.den) o.den[vi] = denom * exp2(-double(s) * k.law.bExp);
+        acc[2 * gid] = make_float4(SN[0], SN[1], SN[2], SD);
+        acc[2 * gid + 1] = make_float4(CN[0], CN[1], CN[2], CD);
     }
-    cnt.flush(o.counters);
+    cnt.flush(counters);
+}
+
+// Normalisation and add-back in FP64: Xv = Xv0 + num/den, and the true-unit
+// denominator den/sigma^b for the derivative.
+__global__ void k_finalize_mixed(VolumeDev v, WalkRecF rec, const float4 *acc, double bExp, double *xv, double *den) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gid >= v.nVol) return;
+    const int vi = v.perm[gid];
+    const float4 a = acc[2 * gid], c = acc[2 * gid + 1];
+    const double N0 = double(a.x) + double(c.x), N1 = double(a.y) + double(c.y), N2 = double(a.z) + double(c.z);
+    const double D = double(a.w) + double(c.w);
+    const double oden = 1.0 / D;
+    if (xv) {
+        xv[3 * vi + 0] = v.xv0[3 * vi + 0] + N0 * oden;
+        xv[3 * vi + 1] = v.xv0[3 * vi + 1] + N1 * oden;
+        xv[3 * vi + 2] = v.xv0[3 * vi + 2] + N2 * oden;
+    }
+    if (den) {
+        const int s = __float_as_int(rec.lo[gid].w);
+        den[vi] = D * exp2(-double(s) * bExp);
+    }
+}
+
+// Set-up: FP32 walk records of every volume node in Morton order and every
+// mirror: the double-float split of the mirrored point, the denominator
+// estimate and the node's weight-scale exponent s (sigma = 2^s, sigma^b ~ 1/den0).
+__global__ void k_walk_records(VolumeDev v, SymPlanes sym, double bExp, float4 *hi, float4 *lo) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gid >= v.nVol) return;
+    const int vi = v.perm[gid];
+    const double x0[3] = {v.xv0[3 * vi], v.xv0[3 * vi + 1], v.xv0[3 * vi + 2]};
+    const double den0 = v.den0[vi];
+    int s = 0;
+    if (den0 > 0.0 && den0 < 1e300) s = max(-40, min(40, int(rint(-double(ilogb(den0)) / bExp))));
+    const float den0f = float(fmin(den0, 3.0e38));
+    for (int kk = 0; kk < sym.nLoop; ++kk) {
+        double r[3];
+        mirror_point(sym, kk, x0, r);
+        float h[3], l[3];
+        for (int c = 0; c < 3; ++c) {
+            h[c] = float(r[c]);
+            l[c] = float(r[c] - double(h[c]));
+        }
+        hi[kk * v.nVol + gid] = make_float4(h[0], h[1], h[2], den0f);
+        lo[kk * v.nVol + gid] = make_float4(l[0], l[1], l[2], __int_as_float(s));
+    }
 }
 
 inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 
 }  // namespace
 
+void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, float4 *hi, float4 *lo,
+                         cudaStream_t st) {
+    if (v.nVol > 0) k_walk_records<<<blocks(v.nVol, 256), 256, 0, st>>>(v, sym, bExp, hi, lo);
+}
+
 void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
-                       const VolumeDev &v, const EvalConsts &k, int exact, const WalkOut &o, cudaStream_t st) {
+                       const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
+                       const WalkOut &o, cudaStream_t st) {
     if (v.nVol <= 0) return;
     const int g = blocks(v.nVol, 128);
+    MixedParams mp;
+    mp.nLoop = k.sym.nLoop;
+    mp.nSym = k.sym.n;
+    for (int j = 0; j < kMaxSym; ++j)
+        for (int c = 0; c < 3; ++c) {
+            mp.nrm[j][c] = j < k.sym.n ? float(k.sym.nrm[j][c]) : 0.f;
+            mp.nrmLo[j][c] = j < k.sym.n ? float(k.sym.nrm[j][c] - double(mp.nrm[j][c])) : 0.f;
+        }
+    mp.LdefF = float(k.law.Ldef);
+    mp.LdefLo = float(k.law.Ldef - double(mp.LdefF));
+    mp.alphaToBexpF = float(k.law.alphaToBexp);
+    mp.abH = mp.alphaToBexpF;
+    mp.abL = float(k.law.alphaToBexp - double(mp.abH));
+    mp.precGate = float(k.precGate);
+    mp.errTolF = float(k.errTol);
+    mp.errTol = k.errTol;
+    mp.intExp = k.law.isInt;
+    mp.dExp = k.law.ib - k.law.ia;
+    mp.dExpF = float(k.law.bExp - k.law.aExp);
+    mp.slotStats = k.slotStats;
     if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         Law32<0> law{3, 5, 3.f, 5.f};
-        k_walk_mixed<0><<<g, 128, 0, st>>>(t, tf, pf, af, v, k, law, exact, o);
+        k_walk_mixed<0><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
     } else if (k.law.isInt) {
         Law32<1> law{k.law.ia, k.law.ib, float(k.law.aExp), float(k.law.bExp)};
-        k_walk_mixed<1><<<g, 128, 0, st>>>(t, tf, pf, af, v, k, law, exact, o);
+        k_walk_mixed<1><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
     } else {
         Law32<2> law{0, 0, float(k.law.aExp), float(k.law.bExp)};
-        k_walk_mixed<2><<<g, 128, 0, st>>>(t, tf, pf, af, v, k, law, exact, o);
+        k_walk_mixed<2><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
     }
+    k_finalize_mixed<<<blocks(v.nVol, 256), 256, 0, st>>>(v, rec, acc, k.law.bExp, o.xv, o.den);
 }
 
 }  // namespace idw

@@ -199,13 +199,14 @@ __global__ void k_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *
     ptDA[i] = make_float4(float(x.x - g.x), float(x.y - g.y), float(x.z - g.z), float(x.w));
 }
 
-// Per warp: D = M - I and u = M Xu0 + b - Xu0 per point, in FP32.
-__global__ void k_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM) {
+// Per warp: D = M - I and u = M Xu0 + b - Xu0 per point, FP32 high and low parts.
+__global__ void k_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, float *ptDMl) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *m = ptMB + 12 * i;
     dbl4 x = ptXA[i];
     float *o = ptDM + 12 * i;
+    float *ol = ptDMl + 12 * i;
     double X[3] = {x.x, x.y, x.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -214,15 +215,18 @@ __global__ void k_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float
         for (int k = 0; k < 3; ++k) {
             double d = m[3 * a + k] - (a == k ? 1.0 : 0.0);
             o[3 * a + k] = float(d);
+            ol[3 * a + k] = float(d - double(float(d)));
             Mx += d * X[k];
         }
-        o[9 + a] = float(Mx + m[9 + a]);
+        double u = Mx + m[9 + a];
+        o[9 + a] = float(u);
+        ol[9 + a] = float(u - double(float(u)));
     }
 }
 
-// Per warp: cluster Dbar = Mbar - I and c = Mbar X + bbar - X in FP32
-// (interior nodes only; leaves are never approximated).
-__global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, float *nodeDC) {
+// Per warp: cluster Dbar = Mbar - I and c = Mbar X + bbar - X as FP32 high
+// and low parts (interior nodes only; leaves are never approximated).
+__global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, float *nodeDC, float *nodeDCl) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= t.nNodes) return;
     if (t.info[q].w) return;
@@ -230,6 +234,7 @@ __global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, float *nodeDC) {
     dbl4 g = t.geom[q];
     double X[3] = {g.x, g.y, g.z};
     float *o = nodeDC + 12 * q;
+    float *ol = nodeDCl + 12 * q;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         double Mx = 0.0;
@@ -237,9 +242,12 @@ __global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, float *nodeDC) {
         for (int k = 0; k < 3; ++k) {
             double d = m[3 * a + k] - (a == k ? 1.0 : 0.0);
             o[3 * a + k] = float(d);
+            ol[3 * a + k] = float(d - double(float(d)));
             Mx += d * X[k];
         }
-        o[9 + a] = float(Mx + m[9 + a]);
+        double cval = Mx + m[9 + a];
+        o[9 + a] = float(cval);
+        ol[9 + a] = float(cval - double(float(cval)));
     }
 }
 
@@ -314,12 +322,12 @@ void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, 
                                                         ptXA, ptDA);
 }
 
-void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, cudaStream_t st) {
-    if (n > 0) k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, ptXA, ptMB, ptDM);
+void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, float *ptDMl, cudaStream_t st) {
+    if (n > 0) k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, ptXA, ptMB, ptDM, ptDMl);
 }
 
-void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, cudaStream_t st) {
-    if (t.nNodes > 0) k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, nodeDC);
+void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, float *nodeDCl, cudaStream_t st) {
+    if (t.nNodes > 0) k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, nodeDC, nodeDCl);
 }
 
 // Sort volume nodes by Morton code (set-up).  perm[k] = common index of the

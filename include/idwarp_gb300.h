@@ -64,7 +64,10 @@ typedef struct idw_options {
     int32_t zeroCornerRotations; /* default 1 */
     int32_t bucketSize;   /* default 8 */
     int32_t precision;    /* IDW_PREC_MIXED (default) or IDW_PREC_FP64 */
-    int32_t reserved[7];
+    int32_t diagnostics;  /* bit 0: count warp-level lane slots in idw_stats */
+    double mixedGate;     /* mixed mode: a term whose weight share x lever arm exceeds
+                           * mixedGate*Ldef is summed in double-float (default 3e-3) */
+    int32_t reserved[4];
 } idw_options;
 
 /* Work counters of the last warp / warpDeriv call. */
@@ -81,7 +84,10 @@ typedef struct idw_stats {
     int64_t nLoop;
     double Ldef0;
     double lastKernelMs;  /* device time of the last evaluation kernel(s) */
-    int64_t reserved[4];
+    int64_t warpLeafSlots; /* lane slots of warp-level leaf visits (32 x leaf size); leafPairs / this = lane use */
+    int64_t warpNodeSlots; /* lane slots of warp-level interior-node visits (32 per visit) */
+    int64_t preciseTerms;  /* mixed mode: cluster terms summed in double-float */
+    int64_t reserved[1];
 } idw_stats;
 
 /* Fill `o` with the reference defaults (idwarp/UnstructuredMesh.py:124-145). */
@@ -173,6 +179,11 @@ int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *d
 /* Denominator estimate denominator0 (nvol), in common order.
  * (initializeWarping.F90:241-247) */
 int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where);
+
+/* Denominator sum(w) of the last idw_warp_mesh (nvol), in common order; the
+ * reference's module variable `denominator` (src/warp/warpMesh.F90:59-70),
+ * used by idw_warp_deriv. */
+int idw_get_denominator(void *ctx, double *out, int64_t nvol, int where);
 
 /* Counters of the last call. */
 int idw_get_stats(void *ctx, idw_stats *out);

