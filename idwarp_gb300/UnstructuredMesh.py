@@ -99,7 +99,7 @@ class USMesh(BaseSolver):
             "restartFile": [(str, type(None)), None],
             "bucketSize": [int, 8],
             "precision": [str, ["mixed", "fp64"]],
-            "mixedGate": [float, 3e-3],
+            "mixedGate": [float, 2e-3],
         }
 
     # ------------------------------------------------------------------

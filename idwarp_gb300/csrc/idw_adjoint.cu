@@ -1,0 +1,294 @@
+// Mixed-precision reverse walk of warpDeriv for S seeds at once.
+//   evalNode_b / evalNodeExact_b / evalNodeApprox_b  src/modules/kd_tree.F90:942-1031
+//   driven as warpDeriv                              src/warp/warpDeriv.F90:71-88
+//   setData_b                                        src/modules/kd_tree.F90:1033-1051
+//
+// Same warp-cooperative walk and the same guarded decisions as the forward
+// mixed walk (decide32 + resolve64), so every lane visits exactly the terms
+// the forward pass used.  A term (surface point i of a leaf, or an
+// approximated cluster q) receives from lane l the contribution
+//     sib = w_l * numb_l (3 per seed),   (r_l - C) (x) sib  (9 per seed),
+// with C the leaf centroid (points) or the cluster centroid (clusters): the
+// moments are kept relative to C so that nothing of size |r| is accumulated
+// and later cancelled.  Writing v_l = w_l (1, r_l - C), the warp's sum over
+// lanes is the small product  V (4 x 32) . N (32 x 3S)  with N the lanes'
+// seeds, which the warp forms from shared memory; one FP64 atomic per result
+// lands it in the per-point / per-cluster accumulators.
+#include "idw_mixed.cuh"
+
+namespace idw {
+
+namespace {
+
+constexpr int kChunk = 8;  // leaf points reduced per shared-memory pass
+
+template <int S>
+struct AdjSmem {
+    float nb[32][3 * S];       // seeds of every lane (numerator adjoints, scaled)
+    float4 vb[kChunk][32];     // per point: w, w (r - C)
+};
+
+// Warp reduction of m point contributions (vb[0..m)) against the lanes'
+// seeds, accumulated into dst(p) + 12 * ... (P row-major then B).
+template <int S>
+__device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *targets, double *adj,
+                                             int64_t seedStride) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    for (int c = lane; c < 3 * S; c += 32) {
+        const int s = c / 3, a = c - 3 * s;
+        float acc[kChunk][4];
+#pragma unroll
+        for (int p = 0; p < kChunk; ++p) acc[p][0] = acc[p][1] = acc[p][2] = acc[p][3] = 0.f;
+        for (int l = 0; l < 32; ++l) {
+            const float nbv = sm.nb[l][c];
+#pragma unroll
+            for (int p = 0; p < kChunk; ++p) {
+                if (p < m) {
+                    const float4 v = sm.vb[p][l];
+                    acc[p][0] = fmaf(v.x, nbv, acc[p][0]);
+                    acc[p][1] = fmaf(v.y, nbv, acc[p][1]);
+                    acc[p][2] = fmaf(v.z, nbv, acc[p][2]);
+                    acc[p][3] = fmaf(v.w, nbv, acc[p][3]);
+                }
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < kChunk; ++p) {
+            if (p < m && acc[p][0] != 0.f) {
+                double *d = adj + s * seedStride + 12 * int64_t(targets[p]);
+                atomicAdd(d + 9 + a, double(acc[p][0]));
+                atomicAdd(d + 3 * a + 0, double(acc[p][1]));
+                atomicAdd(d + 3 * a + 1, double(acc[p][2]));
+                atomicAdd(d + 3 * a + 2, double(acc[p][3]));
+            }
+        }
+    }
+    __syncwarp();
+}
+
+template <int S, int KIND>
+__global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, VolumeDev v,
+                                                       WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
+                                                       const double *dxv, int64_t dxvStride, const double *den,
+                                                       double *ptAdj, int64_t ptStride, double *nodeAdj,
+                                                       int64_t nodeStride, unsigned long long *counters) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    AdjSmem<S> &sm = reinterpret_cast<AdjSmem<S> *>(smraw)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool valid = gid < v.nVol;
+    const int64_t g = valid ? gid : 0;
+    const int vi = v.perm[g];
+    const float4 r0lo = rec.lo[g];
+    const int s = __float_as_int(r0lo.w);
+    const float den0f = rec.hi[g].w;
+    const float Ls = mp.LdefF * pow2f(s);
+    const float LsLo = mp.LdefLo * pow2f(s);
+    const float c1 = mp.intExp ? pow2f(s * mp.dExp) : exp2f(float(s) * mp.dExpF);
+    const float ab = mp.abH, abl = mp.abL;
+    const float tauf = mp.errTolF * den0f;
+    // numb = dXv / den with den in the scaled units of the walk's weights
+    const double q = valid ? exp2(-double(s) * mp.bExp) / den[vi] : 0.0;
+    MixedCounters cnt;
+    int targets[kChunk];
+    for (int kk = 0; kk < mp.nLoop; ++kk) {
+        const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
+        const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
+        // this mirror's seeds: the transpose of the numerator reflection
+        // (getMirrorNumerator_b, src/warp/initializeWarping.F90:603-635)
+        for (int sd = 0; sd < S; ++sd) {
+            const double *dv = dxv + sd * dxvStride + 3 * int64_t(vi);
+            float n3[3] = {valid ? float(dv[0] * q) : 0.f, valid ? float(dv[1] * q) : 0.f,
+                           valid ? float(dv[2] * q) : 0.f};
+#pragma unroll
+            for (int j = kMaxSym - 1; j >= 0; --j) {
+                if (j < mp.nSym && ((kk >> j) & 1)) {
+                    const float dp = n3[0] * mp.nrm[j][0] + n3[1] * mp.nrm[j][1] + n3[2] * mp.nrm[j][2];
+                    n3[0] -= 2.f * dp * mp.nrm[j][0];
+                    n3[1] -= 2.f * dp * mp.nrm[j][1];
+                    n3[2] -= 2.f * dp * mp.nrm[j][2];
+                }
+            }
+            sm.nb[lane][3 * sd] = n3[0];
+            sm.nb[lane][3 * sd + 1] = n3[1];
+            sm.nb[lane][3 * sd + 2] = n3[2];
+        }
+        __syncwarp();
+        int node = 0, skip = 0;
+        while (node < t.nNodes) {
+            const int4 inf = t.info[node];
+            const bool active = valid && node >= skip;
+            if (inf.w) {
+                if (__any_sync(kFull, active)) {
+                    float h0 = 0.f, h1 = 0.f, h2 = 0.f, l0 = 0.f, l1 = 0.f, l2 = 0.f;
+                    if (active) {
+                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+                        two_diff(rh[0], ch.x, h0, l0);
+                        two_diff(rh[1], ch.y, h1, l1);
+                        two_diff(rh[2], ch.z, h2, l2);
+                        l0 += rl[0] - cl.x;
+                        l1 += rl[1] - cl.y;
+                        l2 += rl[2] - cl.z;
+                        cnt.leafPairs += inf.y - inf.x + 1;
+                        cnt.visited++;
+                    }
+                    const float R0 = h0 + l0, R1 = h1 + l1, R2 = h2 + l2;
+                    for (int i0 = inf.x; i0 <= inf.y; i0 += kChunk) {
+                        const int m = min(kChunk, inf.y - i0 + 1);
+                        for (int p = 0; p < m; ++p) {
+                            const int i = i0 + p;
+                            targets[p] = i;
+                            float w = 0.f;
+                            if (active) {
+                                const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
+                                const float dx = (h0 - da.x) + (l0 - dl.x);
+                                const float dy = (h1 - da.y) + (l1 - dl.y);
+                                const float dz = (h2 - da.z) + (l2 - dl.z);
+                                const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
+                                const float r1 = rsqrtf(d2);
+                                w = da.w * law.eval(fmaf(Ls, r1, LsLo * r1), c1, ab, abl);
+                            }
+                            sm.vb[p][lane] = make_float4(w, w * R0, w * R1, w * R2);
+                        }
+                        reduce_terms<S>(sm, m, targets, ptAdj, ptStride);
+                    }
+                }
+                node = inf.z;
+            } else {
+                bool open = false;
+                int dec = 0;
+                float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
+                if (active && !exact) {
+                    cnt.visited++;
+                    dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                }
+                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, cnt.fallback);
+                if (__any_sync(kFull, dec == 1)) {
+                    float w = 0.f;
+                    if (dec == 1) {
+                        w = wA * law.eval(fmaf(Ls, rs, LsLo * rs), c1, ab, abl);
+                        skip = inf.z;
+                        cnt.approx++;
+                    }
+                    targets[0] = node;
+                    sm.vb[0][lane] = make_float4(w, w * rho0, w * rho1, w * rho2);
+                    reduce_terms<S>(sm, 1, targets, nodeAdj, nodeStride);
+                }
+                if (dec != 1 && active) open = true;
+                node = __any_sync(kFull, open) ? node + 1 : inf.z;
+            }
+        }
+        __syncwarp();
+    }
+    cnt.flush(counters);
+}
+
+// Combine the point and cluster moments into the relative adjoints the
+// reverse nodal-property step consumes (setData_b, kd_tree.F90:1033-1051):
+//   Bib_i = B_i + sum_q Bq/n_q
+//   Mrel_i = P_i - (Xu0_i - C_L) (x) B_i + sum_q (Pq + (C_q - Xu0_i) (x) Bq)/n_q
+// where q runs over the interior ancestors of point i.  FP64, one thread per
+// (point, seed).
+__global__ void k_adjoint_combine(TreeDev t, const dbl4 *ptXA, int nPts, int nSeeds, const double *ptAcc,
+                                  int64_t ptStride, const double *nodeAcc, int64_t nodeStride, double *out) {
+    const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (tid >= int64_t(nPts) * nSeeds) return;
+    const int sd = int(tid / nPts), i = int(tid - int64_t(sd) * nPts);
+    const dbl4 x = ptXA[i];
+    const double X[3] = {x.x, x.y, x.z};
+    double B[3] = {0, 0, 0}, M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int q = 0;
+    while (q < t.nNodes) {
+        const int4 inf = t.info[q];
+        if (inf.w) break;
+        const double on = 1.0 / double(inf.y - inf.x + 1);
+        const double *a = nodeAcc + sd * nodeStride + 12 * int64_t(q);
+        const dbl4 g = t.geom[q];
+        const double dc[3] = {g.x - X[0], g.y - X[1], g.z - X[2]};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            B[r] += a[9 + r] * on;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) M[3 * r + k] += (a[3 * r + k] + dc[k] * a[9 + r]) * on;
+        }
+        const int4 li = t.info[q + 1];
+        q = (i <= li.y) ? q + 1 : li.z;
+    }
+    // q is now the leaf of point i
+    const dbl4 g = t.geom[q];
+    const double dl[3] = {X[0] - g.x, X[1] - g.y, X[2] - g.z};
+    const double *p = ptAcc + sd * ptStride + 12 * int64_t(i);
+    double *o = out + sd * ptStride + 12 * int64_t(i);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        o[9 + r] = p[9 + r] + B[r];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) o[3 * r + k] = p[3 * r + k] - dl[k] * p[9 + r] + M[3 * r + k];
+    }
+}
+
+template <int S, int KIND>
+void launch_adj(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
+                const MixedParams &mp, const Law32<KIND> &law, int exact, const double *dxv, int64_t dxvStride,
+                const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj, int64_t nodeStride,
+                unsigned long long *counters, cudaStream_t st) {
+    const size_t smem = 4 * sizeof(AdjSmem<S>);
+    cudaFuncSetAttribute(k_adjoint_mixed<S, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const int g = int((v.nVol + 127) / 128);
+    k_adjoint_mixed<S, KIND><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den, ptAdj,
+                                                   ptStride, nodeAdj, nodeStride, counters);
+}
+
+template <int S>
+void launch_adj_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
+                    const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, int exact, const double *dxv,
+                    int64_t dxvStride, const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj,
+                    int64_t nodeStride, unsigned long long *counters, cudaStream_t st) {
+    if (wl.isInt && wl.ia == 3 && wl.ib == 5) {
+        launch_adj<S, 0>(t, tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, dxv, dxvStride, den, ptAdj, ptStride,
+                         nodeAdj, nodeStride, counters, st);
+    } else if (wl.isInt) {
+        launch_adj<S, 1>(t, tf, pf, v, rec, mp, Law32<1>{wl.ia, wl.ib, float(wl.aExp), float(wl.bExp)}, exact, dxv,
+                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, st);
+    } else {
+        launch_adj<S, 2>(t, tf, pf, v, rec, mp, Law32<2>{0, 0, float(wl.aExp), float(wl.bExp)}, exact, dxv,
+                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, st);
+    }
+}
+
+}  // namespace
+
+int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
+                         const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
+                         int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
+                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st) {
+    if (v.nVol <= 0 || nSeeds <= 0) return 0;
+    const MixedParams mp = make_mixed_params(k);
+    const int64_t ptStride = 12 * int64_t(nPts), nodeStride = 12 * int64_t(t.nNodes);
+    int s0 = 0;
+    while (s0 < nSeeds) {
+        const int left = nSeeds - s0;
+        const double *d = dxv + s0 * dxvStride;
+        double *pa = ptAcc + s0 * ptStride, *na = nodeAcc + s0 * nodeStride;
+        if (left >= 16) {
+            launch_adj_law<16>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
+                               counters, st);
+            s0 += 16;
+        } else if (left >= 4) {
+            launch_adj_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
+                              counters, st);
+            s0 += 4;
+        } else {
+            launch_adj_law<1>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
+                              counters, st);
+            s0 += 1;
+        }
+    }
+    const int64_t total = int64_t(nPts) * nSeeds;
+    k_adjoint_combine<<<int((total + 127) / 128), 128, 0, st>>>(t, ptXA, nPts, nSeeds, ptAcc, ptStride, nodeAcc,
+                                                                nodeStride, ptAdj);
+    return 0;
+}
+
+}  // namespace idw

@@ -234,7 +234,7 @@ void idw_default_options(idw_options *o) {
     o->bucketSize = 8;
     o->precision = IDW_PREC_MIXED;
     o->diagnostics = 0;
-    o->mixedGate = 3e-3;
+    o->mixedGate = 2e-3;
 }
 
 int idw_create(const idw_options *opts, void **ctx_out) {
@@ -778,26 +778,46 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     p.mb = c->ptMB.p;
     const int n = c->nUnique, nn = c->nNodes;
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
-    DevBuf<double> ptAdj, nodeAdj;
+    const int mixed = c->opt.precision == IDW_PREC_MIXED;
+    DevBuf<double> ptAdj, nodeAdj, ptRel;
     CKA(ptAdj.alloc(size_t(nSeeds) * 12 * n));
     CKA(nodeAdj.alloc(size_t(nSeeds) * 12 * nn));
+    if (mixed) CKA(ptRel.alloc(size_t(nSeeds) * 12 * n));
     CK(cudaMemsetAsync(ptAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * n, c->stream));
     CK(cudaMemsetAsync(nodeAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * nn, c->stream));
     CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
-    launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride, ptAdj.p,
-                             nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
+    if (mixed) {
+        TreeDevF tf;
+        tf.cHi = c->cHi.p;
+        tf.cLo = c->cLo.p;
+        tf.aLo = c->nodeALo.p;
+        tf.err = c->errF.p;
+        PointsDevF pf;
+        pf.da = c->ptDA.p;
+        pf.dl = c->ptDL.p;
+        pf.dm = c->ptDM.p;
+        pf.dml = c->ptDMl.p;
+        WalkRecF rec;
+        rec.hi = c->recHi.p;
+        rec.lo = c->recLo.p;
+        launch_adjoint_mixed(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride, c->den.p,
+                             ptAdj.p, nodeAdj.p, ptRel.p, c->ptXA.p, n, c->counters.p, c->stream);
+    } else {
+        launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride,
+                                 ptAdj.p, nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
+    }
     CK(cudaEventRecord(c->ev1, c->stream));
     c->eventsRecorded = true;
     rc = check_launch(c, "adjoint walk");
     if (rc) return rc;
     SurfaceDev s = surf_dev(c);
     for (int sd = 0; sd < nSeeds; ++sd) {
-        double *pa = ptAdj.p + size_t(sd) * 12 * n;
-        launch_set_data_b(tree_dev(c), nodeAdj.p + size_t(sd) * 12 * nn, pa, n, c->stream);
+        double *pa = (mixed ? ptRel.p : ptAdj.p) + size_t(sd) * 12 * n;
+        if (!mixed) launch_set_data_b(tree_dev(c), nodeAdj.p + size_t(sd) * 12 * nn, pa, n, c->stream);
         CK(cudaMemsetAsync(c->xub.p, 0, sizeof(double) * 3 * n, c->stream));
-        launch_nodal_b(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa, c->xub.p,
-                       c->stream);
+        launch_nodal_b(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa, mixed,
+                       c->xub.p, c->stream);
         double *dst = (where == IDW_DEVICE) ? dxsOut + sd * dxsStride : c->dxs.p;
         CK(cudaMemsetAsync(dst, 0, sizeof(double) * 3 * c->nPts, c->stream));
         launch_scatter_dxs(n, c->xuInd.p, c->xub.p, dst, c->stream);

@@ -61,6 +61,7 @@ struct MixedParams {
     float dExpF;
     int slotStats;  // count warp-level lane slots (diagnostics)
     float LdefLo, abH, abL, precGate;
+    double bExp;
 };
 
 struct NodeAggF {
@@ -99,7 +100,8 @@ void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const d
 void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, cudaStream_t st);
 void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st);
 void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
-                    const int *isCorner, int useRotations, const double *ptAdj, double *Xub, cudaStream_t st);
+                    const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
+                    cudaStream_t st);
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st);
 
 // Set-up kernels (idw_setup.cu)
@@ -127,6 +129,11 @@ int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeD
                              int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,
                              double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
                              unsigned long long *counters, cudaStream_t st);
+MixedParams make_mixed_params(const EvalConsts &k);
+int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
+                         const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
+                         int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
+                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st);
 int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
                 cudaStream_t st);
 

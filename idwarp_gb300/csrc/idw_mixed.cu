@@ -17,174 +17,11 @@
 // from the threshold than the FP32 error bound; otherwise they are re-taken
 // with the FP64 decision of the FP64 form (decide64), so the mixed walk makes
 // exactly the FP64 walk's decisions.
-#include "idw_common.cuh"
-#include "idw_kernels.h"
+#include "idw_mixed.cuh"
 
 namespace idw {
 
 namespace {
-
-struct MixedCounters {
-    unsigned long long leafPairs = 0, approx = 0, visited = 0, fallback = 0, leafSlots = 0, nodeSlots = 0, precise = 0;
-    __device__ void flush(unsigned long long *dst) {
-        if (!dst) return;
-        unsigned long long a = warp_sum(leafPairs), b = warp_sum(approx), c = warp_sum(visited),
-                           d = warp_sum(fallback);
-        if ((threadIdx.x & 31) == 0) {
-            if (a) atomicAdd(dst + 0, a);
-            if (b) atomicAdd(dst + 1, b);
-            if (c) atomicAdd(dst + 2, c);
-            if (d) atomicAdd(dst + 3, d);
-            if (leafSlots) atomicAdd(dst + 4, leafSlots);
-            if (nodeSlots) atomicAdd(dst + 5, nodeSlots);
-        }
-        unsigned long long e = warp_sum(precise);
-        if ((threadIdx.x & 31) == 0) {
-            if (e) atomicAdd(dst + 6, e);
-        }
-    }
-};
-
-// Law kinds: 0 = exponents (3,5); 1 = other integer exponents; 2 = real.
-template <int KIND>
-struct Law32 {
-    int ia, ib;
-    float fa, fb;
-    // c1 t^a + (ab + abl) t^b; ab + abl is alpha^b split in two floats so the
-    // FP32 terms carry the same alpha^b as the double-float terms.
-    __device__ __forceinline__ float eval(float t, float c1, float ab, float abl) const {
-        if (KIND == 0) {
-            float t2 = t * t;
-            float t3 = t2 * t;
-            float t5 = t3 * t2;
-            return fmaf(c1, t3, fmaf(ab, t5, abl * t5));
-        } else if (KIND == 1) {
-            float ta = ipowf(t, ia);
-            float tb = ta * ipowf(t, ib - ia);
-            return fmaf(c1, ta, fmaf(ab, tb, abl * tb));
-        } else {
-            return c1 * powf(t, fa) + ab * powf(t, fb);
-        }
-    }
-};
-
-// Compensated summation (Neumaier / Ogita-Rump-Oishi Sum2): the sum is s + c,
-// with every rounding error of the running sum captured exactly by two-sum
-// and collected in c, so the pair is accurate to ~u^2 relative.
-__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
-    const float t = s + x;
-    const float bp = t - s;
-    c += (s - (t - bp)) + (x - bp);
-    s = t;
-}
-
-__device__ __forceinline__ float4 ldgf4(const float4 *p) { return __ldg(p); }
-
-// FP32 error-table interpolation with a bound on its deviation from the FP64
-// value (see the file comment).  dOvrR >= 2 here.  The bracket index follows
-// the radii 2,3,4,5,7.5,10,20,40,...,640: unit steps below 5, then 7.5 and 10,
-// then doublings from 20.  Returns err, sets bnd.
-__device__ __forceinline__ float get_error32(const float *e, float dOvrR, float &bnd) {
-    int i;
-    float r0, r1;
-    if (dOvrR < 5.0f) {
-        i = int(dOvrR) - 2;  // 0..2
-        r0 = float(i + 2);
-        r1 = r0 + 1.0f;
-    } else if (dOvrR < 10.0f) {
-        i = dOvrR < 7.5f ? 3 : 4;
-        r0 = i == 3 ? 5.0f : 7.5f;
-        r1 = i == 3 ? 7.5f : 10.0f;
-    } else if (dOvrR < 20.0f) {
-        i = 5;
-        r0 = 10.0f;
-        r1 = 20.0f;
-    } else if (dOvrR < 640.0f) {
-        // 20 * 2^m <= dOvrR < 20 * 2^(m+1), m = 0..4
-        const int m = ((__float_as_int(dOvrR * 0.05f) >> 23) & 0xff) - 127;
-        i = 6 + m;
-        r0 = 20.0f * float(1 << m);
-        r1 = 2.0f * r0;
-    } else {
-        const float e11 = __ldg(e + kNerr - 1);
-        bnd = 2e-6f * fabsf(e11);
-        return e11;
-    }
-    const float orst = 1.0f / (r1 - r0);
-    const float e0 = __ldg(e + i), e1 = __ldg(e + i + 1);
-    const float fact = (dOvrR - r0) * orst;
-    bnd = 2e-6f * (dOvrR * orst * fabsf(e1 - e0) + fabsf(e0) + fabsf(e1));
-    return (1.0f - fact) * e0 + fact * e1;
-}
-
-// Exact difference a - b as (hi, lo) (Knuth two-sum).
-__device__ __forceinline__ void two_diff(float a, float b, float &hi, float &lo) {
-    hi = a - b;
-    const float bb = hi - a;
-    lo = (a - (hi - bb)) - (b + bb);
-}
-
-// ---- double-float (hi + lo) arithmetic for the precision-critical far-field
-// cluster terms (Dekker/Knuth error-free transformations with FMA) ----
-struct dfl {
-    float h, l;
-};
-__device__ __forceinline__ dfl df_norm(float h, float l) {
-    const float s = h + l;
-    return {s, l - (s - h)};
-}
-__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
-    float s, e;
-    s = a.h + b.h;
-    const float bb = s - a.h;
-    e = (a.h - (s - bb)) + (b.h - bb);
-    e += a.l + b.l;
-    return df_norm(s, e);
-}
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
-    const float p = a.h * b.h;
-    float e = fmaf(a.h, b.h, -p);
-    e = fmaf(a.h, b.l, e);
-    e = fmaf(a.l, b.h, e);
-    return df_norm(p, e);
-}
-__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
-    const float p = a.h * b;
-    float e = fmaf(a.h, b, -p);
-    e = fmaf(a.l, b, e);
-    return df_norm(p, e);
-}
-// 1/sqrt(q) with one Newton step carried in double-float.
-__device__ __forceinline__ dfl df_rsqrt(dfl q) {
-    const float y0 = rsqrtf(q.h);
-    const float t = y0 * y0;
-    const float te = fmaf(y0, y0, -t);  // y0^2 = t + te exactly
-    const float p = q.h * t;
-    float e = fmaf(q.h, t, -p);
-    e = fmaf(q.h, te, e);
-    e = fmaf(q.l, t, e);
-    const float r = (1.0f - p) - e;  // 1 - q y0^2 (1 - p is exact near 1)
-    return df_norm(y0, 0.5f * y0 * r);
-}
-template <int KIND>
-__device__ __forceinline__ dfl df_pow_int(dfl t, int n) {
-    if (KIND == 0 && n == 3) return df_mul(df_mul(t, t), t);
-    dfl r = {1.0f, 0.0f}, b = t;
-    while (n > 0) {
-        if (n & 1) r = df_mul(r, b);
-        n >>= 1;
-        if (n) b = df_mul(b, b);
-    }
-    return r;
-}
-// Compensated accumulation of a double-float term into a pair (s + c).
-__device__ __forceinline__ void kahan_add_df(float &s, float &c, dfl x) {
-    kahan_add(s, c, x.h);
-    kahan_add(s, c, x.l);
-}
-
-// Power of two 2^e as a float (|e| <= 126).
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + max(-126, min(127, e))) << 23); }
 
 template <int KIND>
 __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af,
@@ -311,42 +148,11 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                 bool open = false;
                 int dec = 0;  // 0 open, 1 approximate, 2 undecided in FP32
                 float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
-                if (active) {
-                    if (exact) {
-                        dec = 0;
-                    } else {
-                        cnt.visited++;
-                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
-                        wA = cl.w;
-                        rho0 = (rh[0] - ch.x) + (rl[0] - cl.x);
-                        rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
-                        rho2 = (rh[2] - ch.z) + (rl[2] - cl.z);
-                        d2 = fmaf(rho0, rho0, fmaf(rho1, rho1, rho2 * rho2));
-                        rs = rsqrtf(d2);
-                        const float dOvrR = d2 * rs * ch.w;
-                        if (dOvrR < 2.0f * (1.0f - 4e-6f)) {
-                            dec = 0;
-                        } else if (dOvrR <= 2.0f * (1.0f + 4e-6f)) {
-                            dec = 2;
-                        } else {
-                            float bnd;
-                            float err = get_error32(tf.err + kNerr * node, dOvrR, bnd);
-                            bnd += 1e-6f * tauf;
-                            dec = (err + bnd < tauf) ? 1 : ((err - bnd > tauf) ? 0 : 2);
-                        }
-                    }
+                if (active && !exact) {
+                    cnt.visited++;
+                    dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
                 }
-                // rare: re-take undecided decisions with the FP64 rule (warp-uniform branch)
-                if (__any_sync(kFull, dec == 2)) {
-                    if (dec == 2) {
-                        const int vi = v.perm[g];
-                        double r[3] = {double(rh[0]) + double(rl[0]), double(rh[1]) + double(rl[1]),
-                                       double(rh[2]) + double(rl[2])};
-                        double dist64;
-                        dec = decide64(t.geom[node], t.err + kNerr * node, r, mp.errTol * v.den0[vi], dist64);
-                        cnt.fallback++;
-                    }
-                }
+                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, cnt.fallback);
                 bool precise = false;
                 if (dec == 1) {
                     const float tt = fmaf(Ls, rs, LsLo * rs);
@@ -489,16 +295,7 @@ inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 
 }  // namespace
 
-void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, float4 *hi, float4 *lo,
-                         cudaStream_t st) {
-    if (v.nVol > 0) k_walk_records<<<blocks(v.nVol, 256), 256, 0, st>>>(v, sym, bExp, hi, lo);
-}
-
-void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
-                       const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
-                       const WalkOut &o, cudaStream_t st) {
-    if (v.nVol <= 0) return;
-    const int g = blocks(v.nVol, 128);
+MixedParams make_mixed_params(const EvalConsts &k) {
     MixedParams mp;
     mp.nLoop = k.sym.nLoop;
     mp.nSym = k.sym.n;
@@ -519,6 +316,21 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
     mp.dExp = k.law.ib - k.law.ia;
     mp.dExpF = float(k.law.bExp - k.law.aExp);
     mp.slotStats = k.slotStats;
+    mp.bExp = k.law.bExp;
+    return mp;
+}
+
+void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, float4 *hi, float4 *lo,
+                         cudaStream_t st) {
+    if (v.nVol > 0) k_walk_records<<<blocks(v.nVol, 256), 256, 0, st>>>(v, sym, bExp, hi, lo);
+}
+
+void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                       const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
+                       const WalkOut &o, cudaStream_t st) {
+    if (v.nVol <= 0) return;
+    const int g = blocks(v.nVol, 128);
+    const MixedParams mp = make_mixed_params(k);
     if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         Law32<0> law{3, 5, 3.f, 5.f};
         k_walk_mixed<0><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);

@@ -386,8 +386,10 @@ __global__ void k_set_data_b(TreeDev t, const double *nodeAdj, double *ptAdj, in
 
 // Reverse nodal properties: point adjoints (Mib, Bib) -> Xub; one thread per
 // node, scatter to face vertices with atomics.
+// relative = 1: ptAdj's first nine entries already hold Mib - Xu0 (x) Bib
+// (the mixed adjoint accumulates them that way).
 __global__ void k_nodal_b(SurfaceDev s, const double *Xu, const dbl4 *xa, const double *normals0,
-                          const int *isCorner, int useRotations, const double *ptAdj, double *Xub) {
+                          const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) return;
     const double *adj = ptAdj + 12 * i;
@@ -404,7 +406,7 @@ __global__ void k_nodal_b(SurfaceDev s, const double *Xu, const dbl4 *xa, const 
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) Mb[3 * a + k] = adj[3 * a + k] - x0[k] * Bb[a];
+        for (int k = 0; k < 3; ++k) Mb[3 * a + k] = relative ? adj[3 * a + k] : adj[3 * a + k] - x0[k] * Bb[a];
     double sa, sn[3];
     node_normal(s, Xu, i, sa, sn);
     double nrm[3] = {sn[0] / sa, sn[1] / sa, sn[2] / sa};
@@ -461,9 +463,11 @@ void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, i
     if (nPts > 0) k_set_data_b<<<blocks(nPts, 128), 128, 0, st>>>(t, nodeAdj, ptAdj, nPts);
 }
 void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
-                    const int *isCorner, int useRotations, const double *ptAdj, double *Xub, cudaStream_t st) {
+                    const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
+                    cudaStream_t st) {
     if (s.n > 0)
-        k_nodal_b<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, isCorner, useRotations, ptAdj, Xub);
+        k_nodal_b<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, isCorner, useRotations, ptAdj, relative,
+                                                    Xub);
 }
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st) {
     if (n > 0) k_scatter_dxs<<<blocks(n, 256), 256, 0, st>>>(n, xuInd, Xub, dXs);

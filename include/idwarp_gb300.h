@@ -66,7 +66,7 @@ typedef struct idw_options {
     int32_t precision;    /* IDW_PREC_MIXED (default) or IDW_PREC_FP64 */
     int32_t diagnostics;  /* bit 0: count warp-level lane slots in idw_stats */
     double mixedGate;     /* mixed mode: a term whose weight share x lever arm exceeds
-                           * mixedGate*Ldef is summed in double-float (default 3e-3) */
+                           * mixedGate*Ldef is summed in double-float (default 2e-3) */
     int32_t reserved[4];
 } idw_options;
 

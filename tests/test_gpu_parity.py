@@ -237,3 +237,19 @@ def test_mixed_denominator_feeds_deriv(wing, built_lib, oracle_lib):
     g.warpDeriv(dxv.ravel(), solverVec=False)
     # the mixed denominator carries FP32 rounding (~1e-7 relative per node)
     assert np.abs(g.getdXs() - do).max() <= 1e-6 * np.abs(do).max()
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+def test_mixed_deriv_batch_matches_fp64(mode, wing, built_lib):
+    # the mixed adjoint (S seeds sharing one walk) against the FP64 adjoint
+    g64 = build_gpu(wing, {"evalMode": mode}, precision="fp64")
+    g32 = build_gpu(wing, {"evalMode": mode}, precision="mixed")
+    rng = np.random.default_rng(9)
+    seeds = rng.normal(size=(6,) + wing["xv0"].shape)
+    out = []
+    for g in (g64, g32):
+        g.setSurfaceCoordinates(wing["xs"])
+        g.warpMesh()
+        out.append(g.warpDerivBatch(seeds))
+    scale = np.abs(out[0]).max()
+    assert np.abs(out[1] - out[0]).max() <= 1e-6 * scale, np.abs(out[1] - out[0]).max() / scale
