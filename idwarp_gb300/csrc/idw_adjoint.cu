@@ -117,13 +117,13 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
         __syncwarp();
         int node = 0, skip = 0;
         while (node < t.nNodes) {
-            const int4 inf = t.info[node];
+            const int4 inf = ldgi4(&tf.nodes[node].info);
             const bool active = valid && node >= skip;
             if (inf.w) {
                 if (__any_sync(kFull, active)) {
                     float h0 = 0.f, h1 = 0.f, h2 = 0.f, l0 = 0.f, l1 = 0.f, l2 = 0.f;
                     if (active) {
-                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+                        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                         two_diff(rh[0], ch.x, h0, l0);
                         two_diff(rh[1], ch.y, h1, l1);
                         two_diff(rh[2], ch.z, h2, l2);

@@ -67,9 +67,10 @@ struct Ctx {
     DevBuf<double> nodeErr, nodeAi, nodeMB;
     bool haveTree = false, haveWarp = false, nodalValid = false;
     // FP32 companion arrays of the mixed-precision walk
-    DevBuf<float4> cHi, cLo, ptDA, ptDL;
+    DevBuf<NodeRecF> nodeRec;
+    DevBuf<float4> ptDA, ptDL;
     DevBuf<float4> recHi, recLo, acc;  // per-volume-node walk records and accumulators
-    DevBuf<float> errF, ptDM, ptDMl, nodeDC, nodeDCl, nodeALo;
+    DevBuf<float> ptDM, ptDMl, nodeDC, nodeDCl, nodeDn, refDB;
     // adjoint
     DevBuf<double> ptAdj, nodeAdj, xub, dxs;
     bool haveDxs = false;
@@ -202,8 +203,10 @@ int refresh_nodal(Ctx *c) {
                  c->stream);
     launch_set_data(tree_dev(c), c->ptMB.p, c->nodeMB.p, c->stream);
     if (c->opt.precision == IDW_PREC_MIXED) {
-        launch_mixed_nodal(c->nUnique, c->ptXA.p, c->ptMB.p, c->ptDM.p, c->ptDMl.p, c->stream);
-        launch_mixed_nodes(tree_dev(c), c->nodeMB.p, c->nodeDC.p, c->nodeDCl.p, c->stream);
+        launch_mixed_nodal(c->nUnique, tree_dev(c), c->nodeMB.p, c->ptXA.p, c->ptMB.p, c->ptDM.p, c->ptDMl.p,
+                           c->stream);
+        launch_mixed_nodes(tree_dev(c), c->nodeMB.p, c->ptMB.p, c->nodeDC.p, c->nodeDCl.p, c->nodeDn.p, c->refDB.p,
+                           c->stream);
     }
     c->nodalValid = true;
     return check_launch(c, "nodal properties");
@@ -468,12 +471,11 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->nodeAi.alloc(nn));
     CKA(c->nodeMB.alloc(12 * size_t(nn)));
     CKA(c->nodeAdj.alloc(12 * size_t(nn)));
-    CKA(c->cHi.alloc(nn));
-    CKA(c->cLo.alloc(nn));
-    CKA(c->errF.alloc(kNerr * size_t(nn)));
+    CKA(c->nodeRec.alloc(nn));
     CKA(c->nodeDC.alloc(12 * size_t(nn)));
     CKA(c->nodeDCl.alloc(12 * size_t(nn)));
-    CKA(c->nodeALo.alloc(nn));
+    CKA(c->nodeDn.alloc(nn));
+    CKA(c->refDB.alloc(24));
     CKA(c->ptDA.alloc(n));
     CKA(c->ptDL.alloc(n));
     CKA(c->ptDM.alloc(12 * size_t(n)));
@@ -524,19 +526,27 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     launch_compute_errors(tree_dev(c), c->ptXA.p, law0, c->nodeErr.p, nullptr, 0, st);
     e = check_launch(c, "computeErrors");
     if (e) return e;
-    // FP32 companions: split centroids, radii, areas, error tables, leaf offsets
+    // FP32 companions: node records (split centroid, radius, area, error
+    // table) and leaf-relative point offsets
     {
-        std::vector<float4> hi(nn), lo(nn), da(n), dl(n);
-        std::vector<float> alo(nn);
+        std::vector<double> errH(kNerr * size_t(nn));
+        CK(cudaMemcpyAsync(errH.data(), c->nodeErr.p, sizeof(double) * kNerr * nn, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        std::vector<NodeRecF> recs(nn);
+        std::vector<float4> da(n), dl(n);
         for (int k = 0; k < nn; ++k) {
+            NodeRecF &r = recs[k];
+            std::memset(&r, 0, sizeof(r));
+            r.info = info[k];
             float h[3], l[3];
             for (int q = 0; q < 3; ++q) {
                 h[q] = float(t.X[3 * k + q]);
                 l[q] = float(t.X[3 * k + q] - double(h[q]));
             }
-            hi[k] = make_float4(h[0], h[1], h[2], float(t.oradius[k]));
-            lo[k] = make_float4(l[0], l[1], l[2], float(nodeAi[k]));
-            alo[k] = float(nodeAi[k] - double(float(nodeAi[k])));
+            r.cHi = make_float4(h[0], h[1], h[2], float(t.oradius[k]));
+            r.cLo = make_float4(l[0], l[1], l[2], float(nodeAi[k]));
+            r.aLo = float(nodeAi[k] - double(float(nodeAi[k])));
+            for (int e2 = 0; e2 < kNerr; ++e2) r.err[e2] = float(errH[kNerr * size_t(k) + e2]);
             if (t.leaf[k]) {
                 for (int i = t.l[k]; i <= t.u[k]; ++i) {
                     const double d[3] = {xa[i].x - t.X[3 * k], xa[i].y - t.X[3 * k + 1], xa[i].z - t.X[3 * k + 2]};
@@ -550,12 +560,9 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
                 }
             }
         }
-        CK(cudaMemcpyAsync(c->cHi.p, hi.data(), sizeof(float4) * nn, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(c->cLo.p, lo.data(), sizeof(float4) * nn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(c->nodeRec.p, recs.data(), sizeof(NodeRecF) * nn, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(c->ptDA.p, da.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(c->ptDL.p, dl.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(c->nodeALo.p, alo.data(), sizeof(float) * nn, cudaMemcpyHostToDevice, st));
-        launch_to_float(int64_t(kNerr) * nn, c->nodeErr.p, c->errF.p, st);
         CK(cudaStreamSynchronize(st));
     }
     // denominator estimate over the mirrors (initializeWarping.F90:241-247)
@@ -628,10 +635,7 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     if (c->opt.precision == IDW_PREC_MIXED) {
         TreeDevF tf;
-        tf.cHi = c->cHi.p;
-        tf.cLo = c->cLo.p;
-        tf.aLo = c->nodeALo.p;
-        tf.err = c->errF.p;
+        tf.nodes = c->nodeRec.p;
         PointsDevF pf;
         pf.da = c->ptDA.p;
         pf.dl = c->ptDL.p;
@@ -640,6 +644,8 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
         NodeAggF af;
         af.dc = c->nodeDC.p;
         af.dcl = c->nodeDCl.p;
+        af.dn = c->nodeDn.p;
+        af.ref = c->refDB.p;
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
@@ -789,10 +795,7 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     CK(cudaEventRecord(c->ev0, c->stream));
     if (mixed) {
         TreeDevF tf;
-        tf.cHi = c->cHi.p;
-        tf.cLo = c->cLo.p;
-        tf.aLo = c->nodeALo.p;
-        tf.err = c->errF.p;
+        tf.nodes = c->nodeRec.p;
         PointsDevF pf;
         pf.da = c->ptDA.p;
         pf.dl = c->ptDL.p;

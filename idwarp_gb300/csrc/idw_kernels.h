@@ -25,12 +25,19 @@ struct TreeDev {
     const double *ai;     // per node
 };
 
-// FP32 companion arrays of the mixed-precision path (set-up constants).
+// Everything the mixed walks read at a tree node, packed in one 128-byte
+// record (one cache line per visit).  Set-up constant.
+struct __align__(128) NodeRecF {
+    int4 info;       // l, u, escape, isLeaf (as TreeDev::info)
+    float4 cHi;      // centroid high part, oradius
+    float4 cLo;      // centroid low part, node area A (high part)
+    float err[12];   // error table (true weight units)
+    float aLo;       // node area A, low part
+    float pad[7];
+};
+
 struct TreeDevF {
-    const float4 *cHi;   // centroid high part, oradius
-    const float4 *cLo;   // centroid low part, node area A (high part)
-    const float *aLo;    // node area A, low part
-    const float *err;    // 12 per node (true weight units)
+    const NodeRecF *nodes;
 };
 
 // Surface point data for the evaluation kernels, tree order.
@@ -42,7 +49,7 @@ struct PointsDev {
 struct PointsDevF {
     const float4 *da;    // Xu0 - centroid(leaf) high part, Ai  (FP32, set-up constant)
     const float4 *dl;    // Xu0 - centroid(leaf) low part, Ai low part
-    const float *dm;     // 12 per point: D = M - I (9), u = M Xu0 + b - Xu0 (3), high parts
+    const float *dm;     // 12 per point: D' = M - I - Dref (9), u' = S'(Xu0) (3), high parts
     const float *dml;    // the same, low parts
 };
 
@@ -65,8 +72,10 @@ struct MixedParams {
 };
 
 struct NodeAggF {
-    const float *dc;     // 12 per node: Dbar = Mbar - I (9), c = Mbar X + bbar - X (3), high parts
+    const float *dc;     // 12 per node: D' = Mbar - I - Dref (9), c' = S'(X) (3), high parts
     const float *dcl;    // the same, low parts
+    const float *dn;     // per node: bound on |D'| (max absolute row sum)
+    const float *ref;    // reference motion Dref (9), bref (3): high parts, then low parts
 };
 
 struct VolumeDev {
@@ -113,8 +122,10 @@ void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, cons
                          unsigned long long *codes, int *idx, cudaStream_t st);
 void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, const double *nodeX,
                          float4 *ptDA, cudaStream_t st);
-void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, float *ptDMl, cudaStream_t st);
-void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, float *nodeDCl, cudaStream_t st);
+void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
+                        float *ptDM, float *ptDMl, cudaStream_t st);
+void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
+                        float *nodeDn, float *refDB, cudaStream_t st);
 
 // Evaluation (idw_walk.cu)
 void launch_walk_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const double *nodeMB,

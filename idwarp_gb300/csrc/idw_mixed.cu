@@ -23,8 +23,13 @@ namespace idw {
 
 namespace {
 
+// Resident blocks per SM the register allocation targets (128 threads each).
+#ifndef IDW_WALK_MIN_BLOCKS
+#define IDW_WALK_MIN_BLOCKS 8
+#endif
+
 template <int KIND>
-__global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af,
+__global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af,
                                                     VolumeDev v, WalkRecF rec, MixedParams mp, Law32<KIND> law,
                                                     int exact, float4 *acc, unsigned long long *counters) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -39,7 +44,11 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
     const float c1 = mp.intExp ? pow2f(s * mp.dExp) : exp2f(float(s) * mp.dExpF);
     const float ab = mp.abH, abl = mp.abL;
     const float tauf = mp.errTolF * den0f;
-    float SN[3] = {0, 0, 0}, CN[3] = {0, 0, 0}, SD = 0.f, CD = 0.f;
+    // running sums over the mirrors (sum = S + C per component), kept in shared
+    // memory between mirror passes to free registers for the walk
+    __shared__ float4 mirS[128], mirC[128];
+    mirS[threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+    mirC[threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
     MixedCounters cnt;
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
@@ -47,18 +56,18 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
         float sn[3] = {0, 0, 0}, cn[3] = {0, 0, 0}, sd = 0.f, cd = 0.f;
         int node = 0, skip = 0;
         while (node < t.nNodes) {
-            const int4 inf = t.info[node];
+            const int4 inf = ldgi4(&tf.nodes[node].info);
             const bool active = valid && node >= skip;
             if (mp.slotStats && __any_sync(kFull, active)) {
                 if (inf.w)
-                    cnt.leafSlots += 32ull * (inf.y - inf.x + 1);
+                    cnt.leafSlots += 32u * (inf.y - inf.x + 1);
                 else
-                    cnt.nodeSlots += 32ull;
+                    cnt.nodeSlots += 32u;
             }
             if (inf.w) {
                 bool leafPrecise = false;
                 if (active) {
-                    const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+                    const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                     // r - C as hi + lo: exact high parts, so a volume node on a
                     // surface node resolves d^2 = eps (1e-15) to full precision
                     float h0, h1, h2, l0, l1, l2;
@@ -91,9 +100,13 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                     }
                     // a leaf carrying a large weight share at a long lever arm is
                     // re-summed in double-float (same gate as cluster terms)
-                    leafPrecise = KIND != 2 &&
-                                  fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + 0.1f * pd * sqrtf(h0 * h0 + h1 * h1 + h2 * h2) >
-                                      mp.precGate;
+                    const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) +
+                                       pd * __ldg(af.dn + node) * (fabsf(h0) + fabsf(h1) + fabsf(h2));
+                    const float ldev = sd > 0.f ? lmag * sd + fabsf(fmaf(pn0, sd, -pd * sn[0])) +
+                                                      fabsf(fmaf(pn1, sd, -pd * sn[1])) +
+                                                      fabsf(fmaf(pn2, sd, -pd * sn[2]))
+                                                : lmag;
+                    leafPrecise = KIND != 2 && ldev > mp.precGate * (sd > 0.f ? sd : 1.f);
                     if (!leafPrecise) {
                         kahan_add(sn[0], cn[0], pn0);
                         kahan_add(sn[1], cn[1], pn1);
@@ -105,7 +118,7 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                 }
                 if (__any_sync(kFull, leafPrecise)) {
                     if (leafPrecise) {
-                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+                        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                         dfl q0, q1, q2;
                         two_diff(rh[0], ch.x, q0.h, q0.l);
                         two_diff(rh[1], ch.y, q1.h, q1.l);
@@ -115,30 +128,15 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                         q2.l += rl[2] - cl.z;
                         for (int i = inf.x; i <= inf.y; ++i) {
                             const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
-                            dfl x0, x1, x2;
-                            two_diff(q0.h, da.x, x0.h, x0.l);
-                            two_diff(q1.h, da.y, x1.h, x1.l);
-                            two_diff(q2.h, da.z, x2.h, x2.l);
-                            x0 = df_norm(x0.h, x0.l + (q0.l - dl.x));
-                            x1 = df_norm(x1.h, x1.l + (q1.l - dl.y));
-                            x2 = df_norm(x2.h, x2.l + (q2.l - dl.z));
-                            const dfl d2d = df_add(df_add(df_add(df_mul(x0, x0), df_mul(x1, x1)), df_mul(x2, x2)),
-                                                   {1e-15f, 0.f});
-                            const dfl tt = df_mul({Ls, LsLo}, df_rsqrt(d2d));
-                            const dfl ta = df_pow_int<KIND>(tt, law.ia);
-                            const dfl tb = df_mul(ta, df_pow_int<KIND>(tt, law.ib - law.ia));
-                            const dfl lawv = df_add({c1 * ta.h, c1 * ta.l}, df_mul(tb, {mp.abH, mp.abL}));
-                            const dfl w = df_mul(lawv, {da.w, dl.w});
-                            const float *mh = pf.dm + 12 * i, *ml = pf.dml + 12 * i;
-#pragma unroll
-                            for (int a = 0; a < 3; ++a) {
-                                dfl acc = {__ldg(mh + 9 + a), __ldg(ml + 9 + a)};
-                                acc = df_add(acc, df_mul({__ldg(mh + 3 * a), __ldg(ml + 3 * a)}, x0));
-                                acc = df_add(acc, df_mul({__ldg(mh + 3 * a + 1), __ldg(ml + 3 * a + 1)}, x1));
-                                acc = df_add(acc, df_mul({__ldg(mh + 3 * a + 2), __ldg(ml + 3 * a + 2)}, x2));
-                                kahan_add_df(sn[a], cn[a], df_mul(w, acc));
-                            }
-                            kahan_add_df(sd, cd, w);
+                            dfl x[3];
+                            two_diff(q0.h, da.x, x[0].h, x[0].l);
+                            two_diff(q1.h, da.y, x[1].h, x[1].l);
+                            two_diff(q2.h, da.z, x[2].h, x[2].l);
+                            x[0].l += q0.l - dl.x;
+                            x[1].l += q1.l - dl.y;
+                            x[2].l += q2.l - dl.z;
+                            precise_term<KIND>(x, 1e-15f, da.w, dl.w, pf.dm + 12 * i, pf.dml + 12 * i, law, Ls, LsLo,
+                                               c1, mp.abH, mp.abL, sn, cn, sd, cd);
                         }
                         cnt.precise += inf.y - inf.x + 1;
                     }
@@ -165,7 +163,14 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                     // A far cluster whose share of the weight times its lever arm
                     // is large enough for FP32 rounding to show in Xv is
                     // re-evaluated in double-float below.
-                    precise = KIND != 2 && w * (fabsf(S0) + fabsf(S1) + fabsf(S2) + 0.1f * d2 * rs) > mp.precGate;
+                    // FP32 rounding error of this term in Xv ~ u * w (|S| + |S - num/den|) / den:
+                    // the size of S plus its deviation from the running average
+                    const float mag = fabsf(S0) + fabsf(S1) + fabsf(S2) +
+                                      __ldg(af.dn + node) * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
+                    const float dev = sd > 0.f ? mag * sd + fabsf(fmaf(S0, sd, -sn[0])) +
+                                                     fabsf(fmaf(S1, sd, -sn[1])) + fabsf(fmaf(S2, sd, -sn[2]))
+                                               : mag;
+                    precise = KIND != 2 && w * dev > mp.precGate * (sd > 0.f ? sd : 1.f);
                     if (!precise) {
                         kahan_add(sn[0], cn[0], w * S0);
                         kahan_add(sn[1], cn[1], w * S1);
@@ -179,47 +184,40 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                 }
                 if (__any_sync(kFull, precise)) {
                     if (precise) {
-                        const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
-                        dfl q0, q1, q2;
-                        two_diff(rh[0], ch.x, q0.h, q0.l);
-                        two_diff(rh[1], ch.y, q1.h, q1.l);
-                        two_diff(rh[2], ch.z, q2.h, q2.l);
-                        q0 = df_norm(q0.h, q0.l + (rl[0] - cl.x));
-                        q1 = df_norm(q1.h, q1.l + (rl[1] - cl.y));
-                        q2 = df_norm(q2.h, q2.l + (rl[2] - cl.z));
-                        const dfl d2d = df_add(df_add(df_mul(q0, q0), df_mul(q1, q1)), df_mul(q2, q2));
-                        const dfl tt = df_mul({Ls, LsLo}, df_rsqrt(d2d));
-                        const dfl ta = df_pow_int<KIND>(tt, law.ia);
-                        const dfl tb = df_mul(ta, df_pow_int<KIND>(tt, law.ib - law.ia));
-                        const dfl lawv = df_add({c1 * ta.h, c1 * ta.l}, df_mul(tb, {mp.abH, mp.abL}));
-                        const dfl w = df_mul(lawv, {cl.w, __ldg(tf.aLo + node)});
-                        const float *dh = af.dc + 12 * node, *dlo = af.dcl + 12 * node;
-                        dfl S[3];
-#pragma unroll
-                        for (int a = 0; a < 3; ++a) {
-                            dfl acc = {__ldg(dh + 9 + a), __ldg(dlo + 9 + a)};
-                            acc = df_add(acc, df_mul({__ldg(dh + 3 * a), __ldg(dlo + 3 * a)}, q0));
-                            acc = df_add(acc, df_mul({__ldg(dh + 3 * a + 1), __ldg(dlo + 3 * a + 1)}, q1));
-                            acc = df_add(acc, df_mul({__ldg(dh + 3 * a + 2), __ldg(dlo + 3 * a + 2)}, q2));
-                            S[a] = acc;
-                        }
-                        kahan_add_df(sn[0], cn[0], df_mul(w, S[0]));
-                        kahan_add_df(sn[1], cn[1], df_mul(w, S[1]));
-                        kahan_add_df(sn[2], cn[2], df_mul(w, S[2]));
-                        kahan_add_df(sd, cd, w);
+                        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+                        dfl q[3];
+                        two_diff(rh[0], ch.x, q[0].h, q[0].l);
+                        two_diff(rh[1], ch.y, q[1].h, q[1].l);
+                        two_diff(rh[2], ch.z, q[2].h, q[2].l);
+                        q[0].l += rl[0] - cl.x;
+                        q[1].l += rl[1] - cl.y;
+                        q[2].l += rl[2] - cl.z;
+                        precise_term<KIND>(q, 0.f, cl.w, __ldg(&tf.nodes[node].aLo), af.dc + 12 * node,
+                                           af.dcl + 12 * node, law, Ls, LsLo, c1, mp.abH, mp.abL, sn, cn, sd, cd);
                         cnt.precise++;
                     }
                 }
                 node = __any_sync(kFull, open) ? node + 1 : inf.z;
             }
         }
+        // add the reference motion back: num += den (Dref r + bref), with r
+        // this mirror's point, in double-float
+        const dfl den = df_norm(sd, cd);
+        dfl num[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            dfl sr = {__ldg(af.ref + 9 + a), __ldg(af.ref + 21 + a)};
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                sr = df_add(sr, df_mul({__ldg(af.ref + 3 * a + k), __ldg(af.ref + 12 + 3 * a + k)}, {rh[k], rl[k]}));
+            num[a] = df_add(df_norm(sn[a], cn[a]), df_mul(den, sr));
+        }
         // reflect this mirror's numerator back (vector reflection) and
         // accumulate, all in double-float so no digits are lost between mirrors
         if (mp.nLoop == 1) {
-            SN[0] = sn[0]; SN[1] = sn[1]; SN[2] = sn[2]; SD = sd;
-            CN[0] = cn[0]; CN[1] = cn[1]; CN[2] = cn[2]; CD = cd;
+            mirS[threadIdx.x] = make_float4(num[0].h, num[1].h, num[2].h, den.h);
+            mirC[threadIdx.x] = make_float4(num[0].l, num[1].l, num[2].l, den.l);
         } else {
-            dfl num[3] = {df_norm(sn[0], cn[0]), df_norm(sn[1], cn[1]), df_norm(sn[2], cn[2])};
 #pragma unroll
             for (int j = 0; j < kMaxSym; ++j) {
                 if (j < mp.nSym && ((kk >> j) & 1)) {
@@ -232,15 +230,18 @@ __global__ void __launch_bounds__(128) k_walk_mixed(TreeDev t, TreeDevF tf, Poin
                     num[2] = df_add(num[2], df_mul(dp, n2));
                 }
             }
-            kahan_add_df(SN[0], CN[0], num[0]);
-            kahan_add_df(SN[1], CN[1], num[1]);
-            kahan_add_df(SN[2], CN[2], num[2]);
-            kahan_add_df(SD, CD, df_norm(sd, cd));
+            float4 S4 = mirS[threadIdx.x], C4 = mirC[threadIdx.x];
+            kahan_add_df(S4.x, C4.x, num[0]);
+            kahan_add_df(S4.y, C4.y, num[1]);
+            kahan_add_df(S4.z, C4.z, num[2]);
+            kahan_add_df(S4.w, C4.w, den);
+            mirS[threadIdx.x] = S4;
+            mirC[threadIdx.x] = C4;
         }
     }
     if (valid) {
-        acc[2 * gid] = make_float4(SN[0], SN[1], SN[2], SD);
-        acc[2 * gid + 1] = make_float4(CN[0], CN[1], CN[2], CD);
+        acc[2 * gid] = mirS[threadIdx.x];
+        acc[2 * gid + 1] = mirC[threadIdx.x];
     }
     cnt.flush(counters);
 }

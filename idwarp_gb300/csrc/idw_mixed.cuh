@@ -7,23 +7,16 @@
 
 namespace idw {
 
+// Per-lane work counters (32-bit per lane; summed in 64 bits per warp).
 struct MixedCounters {
-    unsigned long long leafPairs = 0, approx = 0, visited = 0, fallback = 0, leafSlots = 0, nodeSlots = 0, precise = 0;
+    unsigned leafPairs = 0, approx = 0, visited = 0, fallback = 0, leafSlots = 0, nodeSlots = 0, precise = 0;
     __device__ void flush(unsigned long long *dst) {
         if (!dst) return;
-        unsigned long long a = warp_sum(leafPairs), b = warp_sum(approx), c = warp_sum(visited),
-                           d = warp_sum(fallback);
-        if ((threadIdx.x & 31) == 0) {
-            if (a) atomicAdd(dst + 0, a);
-            if (b) atomicAdd(dst + 1, b);
-            if (c) atomicAdd(dst + 2, c);
-            if (d) atomicAdd(dst + 3, d);
-            if (leafSlots) atomicAdd(dst + 4, leafSlots);
-            if (nodeSlots) atomicAdd(dst + 5, nodeSlots);
-        }
-        unsigned long long e = warp_sum(precise);
-        if ((threadIdx.x & 31) == 0) {
-            if (e) atomicAdd(dst + 6, e);
+        const unsigned long long v[7] = {leafPairs, approx, visited, fallback, leafSlots, nodeSlots, precise};
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const unsigned long long s = warp_sum(v[k]);
+            if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst + k, s);
         }
     }
 };
@@ -62,6 +55,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 }
 
 __device__ __forceinline__ float4 ldgf4(const float4 *p) { return __ldg(p); }
+__device__ __forceinline__ int4 ldgi4(const int4 *p) { return __ldg(p); }
 
 // FP32 error-table interpolation with a bound on its deviation from the FP64
 // value (see the file comment).  dOvrR >= 2 here.  The bracket index follows
@@ -166,13 +160,120 @@ __device__ __forceinline__ void kahan_add_df(float &s, float &c, dfl x) {
     kahan_add(s, c, x.l);
 }
 
+// Knuth two-sum: a + b = s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+// Accumulate a double-float value (h + l) into the compensated pair (s + c).
+__device__ __forceinline__ void comp_add_df(float &s, float &c, float h, float l) {
+    float e;
+    two_sum(s, h, s, e);
+    c += e + l;
+}
+
+// One term of the IDW sums in double-float, for terms whose FP32 rounding
+// would show in Xv: x (hi + lo) is the volume point relative to the term's
+// reference point (a surface point, or a cluster centroid), eps the distance
+// softening (1e-15 for surface points, 0 for clusters), A (hi + lo) the area,
+// and S = D x + c with D (9) and c (3) from the hi/lo arrays dh, dl.  Adds
+// w S and w to the compensated pairs.  Specialised to the default exponents
+// (3, 5); others go through the generic double-float routines.
+template <int KIND>
+__device__ __forceinline__ void precise_term(const dfl xin[3], float eps, float Ah, float Al, const float *dh,
+                                             const float *dl, const Law32<KIND> &law, float Ls, float LsLo, float c1,
+                                             float abH, float abL, float *sn, float *cn, float &sd, float &cd) {
+    // x arrives as an exact difference plus a correction that can be as
+    // large as the difference itself (a volume node on a surface node:
+    // hi = -lo); renormalise so that |lo| <= ulp(hi) / 2, which the
+    // products below assume (they drop lo * lo)
+    dfl x[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) two_sum(xin[k].h, xin[k].l, x[k].h, x[k].l);
+    float wh, wl;
+    if (KIND == 0) {
+        // d^2 = |x|^2 + eps
+        const float p0 = x[0].h * x[0].h, p1 = x[1].h * x[1].h, p2 = x[2].h * x[2].h;
+        const float e0 = fmaf(x[0].h, x[0].h, -p0), e1 = fmaf(x[1].h, x[1].h, -p1), e2 = fmaf(x[2].h, x[2].h, -p2);
+        float s1, f1, s2, f2;
+        two_sum(p0, p1, s1, f1);
+        two_sum(s1, p2, s2, f2);
+        // the softening eps can be as large as |x|^2 (a volume node on a
+        // surface node): add it with an exact two-sum, collect every rounding
+        // error in the low part, then renormalise so that |dl| is below half
+        // an ulp of dh, which the Newton residual below relies on
+        float s3, f3;
+        two_sum(s2, eps, s3, f3);
+        const float lo0 = ((e0 + e1) + (e2 + f1)) + (f2 + f3) +
+                          2.f * fmaf(x[0].h, x[0].l, fmaf(x[1].h, x[1].l, x[2].h * x[2].l));
+        float dh2, dl2;
+        two_sum(s3, lo0, dh2, dl2);
+        // y = 1/sqrt(d^2): FP32 seed, one Newton step carried in double-float
+        const float y0 = rsqrtf(dh2);
+        const float t = y0 * y0, te = fmaf(y0, y0, -t);
+        const float p = dh2 * t;
+        float e = fmaf(dh2, t, -p);
+        e = fmaf(dh2, te, e);
+        e = fmaf(dl2, t, e);
+        const float y1 = 0.5f * y0 * ((1.0f - p) - e);
+        // t = L y and its powers (unnormalised double-float products)
+        const float th = Ls * y0;
+        float tl = fmaf(Ls, y0, -th);
+        tl = fmaf(Ls, y1, fmaf(LsLo, y0, tl));
+        const float t2h = th * th;
+        const float t2l = fmaf(2.f * th, tl, fmaf(th, th, -t2h));
+        const float t3h = t2h * th;
+        const float t3l = fmaf(t2l, th, fmaf(t2h, tl, fmaf(t2h, th, -t3h)));
+        const float t5h = t3h * t2h;
+        const float t5l = fmaf(t3l, t2h, fmaf(t3h, t2l, fmaf(t3h, t2h, -t5h)));
+        // law = c1 t^3 + alpha^b t^5, then w = A law
+        const float bh = abH * t5h;
+        const float bl = fmaf(abL, t5h, fmaf(abH, t5l, fmaf(abH, t5h, -bh)));
+        float lh, ll;
+        two_sum(c1 * t3h, bh, lh, ll);
+        ll += fmaf(c1, t3l, bl);
+        wh = Ah * lh;
+        wl = fmaf(Al, lh, fmaf(Ah, ll, fmaf(Ah, lh, -wh)));
+    } else {
+        dfl d2 = df_add(df_add(df_add(df_mul(x[0], x[0]), df_mul(x[1], x[1])), df_mul(x[2], x[2])), {eps, 0.f});
+        const dfl tt = df_mul({Ls, LsLo}, df_rsqrt(d2));
+        const dfl ta = df_pow_int<KIND>(tt, law.ia);
+        const dfl tb = df_mul(ta, df_pow_int<KIND>(tt, law.ib - law.ia));
+        const dfl lawv = df_add({c1 * ta.h, c1 * ta.l}, df_mul(tb, {abH, abL}));
+        const dfl w = df_mul(lawv, {Ah, Al});
+        wh = w.h;
+        wl = w.l;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // S_a = c_a + sum_k D_ak x_k, each product split exactly, sums by two-sum
+        float Sh = __ldg(dh + 9 + a), Sl = __ldg(dl + 9 + a);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float Dh = __ldg(dh + 3 * a + k), Dl = __ldg(dl + 3 * a + k);
+            const float ph = Dh * x[k].h;
+            const float pl = fmaf(Dl, x[k].h, fmaf(Dh, x[k].l, fmaf(Dh, x[k].h, -ph)));
+            float er;
+            two_sum(Sh, ph, Sh, er);
+            Sl += er + pl;
+        }
+        // w S (double-float product) into the running pair
+        const float qh = wh * Sh;
+        const float ql = fmaf(wl, Sh, fmaf(wh, Sl, fmaf(wh, Sh, -qh)));
+        comp_add_df(sn[a], cn[a], qh, ql);
+    }
+    comp_add_df(sd, cd, wh, wl);
+}
+
 // Interior-node decision of the mixed walks from the FP32 records.  Returns 0
 // (open), 1 (approximate) or 2 (too close to a threshold for FP32: the caller
 // re-takes it with decide64).  Also returns r - C (FP32), |r - C|^2, its
 // reciprocal square root and the node area, which the approximation needs.
 __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const float *rh, const float *rl, float tauf,
                                         float &rho0, float &rho1, float &rho2, float &d2, float &rs, float &wA) {
-    const float4 ch = ldgf4(tf.cHi + node), cl = ldgf4(tf.cLo + node);
+    const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
     wA = cl.w;
     rho0 = (rh[0] - ch.x) + (rl[0] - cl.x);
     rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
@@ -183,7 +284,7 @@ __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const floa
     if (dOvrR < 2.0f * (1.0f - 4e-6f)) return 0;
     if (dOvrR <= 2.0f * (1.0f + 4e-6f)) return 2;
     float bnd;
-    const float err = get_error32(tf.err + kNerr * node, dOvrR, bnd);
+    const float err = get_error32(tf.nodes[node].err, dOvrR, bnd);
     bnd += 1e-6f * tauf;
     return (err + bnd < tauf) ? 1 : ((err - bnd > tauf) ? 0 : 2);
 }
@@ -191,7 +292,7 @@ __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const floa
 // Re-take undecided decisions with the FP64 rule (all lanes of the warp call
 // this; the FP64 work runs only when some lane needs it).
 __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const VolumeDev &v, int64_t g, int node,
-                                         const float *rh, const float *rl, double errTol, unsigned long long &fallback) {
+                                         const float *rh, const float *rl, double errTol, unsigned &fallback) {
     if (__any_sync(kFull, dec == 2)) {
         if (dec == 2) {
             const int vi = v.perm[g];

@@ -199,10 +199,35 @@ __global__ void k_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *
     ptDA[i] = make_float4(float(x.x - g.x), float(x.y - g.y), float(x.z - g.z), float(x.w));
 }
 
-// Per warp: D = M - I and u = M Xu0 + b - Xu0 per point, FP32 high and low parts.
-__global__ void k_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, float *ptDMl) {
+// Reference motion of the mixed walk: Dref = Mbar - I and bref = bbar of the
+// root cluster (the mean over all surface points), or zero when the root is a
+// leaf.  The walk sums S - Sref(r) in FP32, where Sref(r) = Dref r + bref, and
+// adds den * Sref(r) back in double-float: the weighted mean is unchanged,
+// while the FP32 rounding scales with how far each term's motion departs from
+// the mean motion (a rigid rotation of the whole surface leaves nothing).
+__device__ __forceinline__ void ref_motion(const TreeDev &t, const double *nodeMB, double Dr[9], double br[3]) {
+    const bool leafRoot = t.info[0].w != 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) Dr[3 * a + k] = leafRoot ? 0.0 : nodeMB[3 * a + k] - (a == k ? 1.0 : 0.0);
+        br[a] = leafRoot ? 0.0 : nodeMB[9 + a];
+    }
+}
+
+__device__ __forceinline__ void split_store(double v, float *hi, float *lo) {
+    *hi = float(v);
+    *lo = float(v - double(float(v)));
+}
+
+// Per point: D' = M - I - Dref and u' = S'(Xu0) = (M - I) Xu0 + b - Dref Xu0 - bref,
+// FP32 high and low parts.
+__global__ void k_mixed_nodal(int n, TreeDev t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
+                              float *ptDM, float *ptDMl) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    double Dr[9], br[3];
+    ref_motion(t, nodeMB, Dr, br);
     const double *m = ptMB + 12 * i;
     dbl4 x = ptXA[i];
     float *o = ptDM + 12 * i;
@@ -213,42 +238,64 @@ __global__ void k_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float
         double Mx = 0.0;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            double d = m[3 * a + k] - (a == k ? 1.0 : 0.0);
-            o[3 * a + k] = float(d);
-            ol[3 * a + k] = float(d - double(float(d)));
+            double d = m[3 * a + k] - (a == k ? 1.0 : 0.0) - Dr[3 * a + k];
+            split_store(d, o + 3 * a + k, ol + 3 * a + k);
             Mx += d * X[k];
         }
-        double u = Mx + m[9 + a];
-        o[9 + a] = float(u);
-        ol[9 + a] = float(u - double(float(u)));
+        split_store(Mx + (m[9 + a] - br[a]), o + 9 + a, ol + 9 + a);
     }
 }
 
-// Per warp: cluster Dbar = Mbar - I and c = Mbar X + bbar - X as FP32 high
-// and low parts (interior nodes only; leaves are never approximated).
-__global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, float *nodeDC, float *nodeDCl) {
+// Per node: cluster D' = Mbar - I - Dref and c' = S'(C) = (Mbar - I) C + bbar -
+// Dref C - bref as FP32 high and low parts (interior nodes), and for every node
+// a bound on |D'| (the largest absolute row sum of the cluster's D', or of the
+// members' D' for a leaf) that sizes the FP32 rounding of D' (r - C) in the
+// walk's precision gate.  Thread 0 also stores the reference motion (Dref 9,
+// bref 3; high parts then low parts) that the walk adds back.
+__global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
+                              float *nodeDn, float *refDB) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= t.nNodes) return;
-    if (t.info[q].w) return;
+    double Dr[9], br[3];
+    ref_motion(t, nodeMB, Dr, br);
+    if (q == 0) {
+        for (int j = 0; j < 9; ++j) split_store(Dr[j], refDB + j, refDB + 12 + j);
+        for (int a = 0; a < 3; ++a) split_store(br[a], refDB + 9 + a, refDB + 21 + a);
+    }
+    const int4 inf = t.info[q];
+    if (inf.w) {
+        double dn = 0.0;
+        for (int i = inf.x; i <= inf.y; ++i) {
+            const double *m = ptMB + 12 * i;
+            for (int a = 0; a < 3; ++a) {
+                double rs = 0.0;
+                for (int k = 0; k < 3; ++k) rs += fabs(m[3 * a + k] - (a == k ? 1.0 : 0.0) - Dr[3 * a + k]);
+                dn = fmax(dn, rs);
+            }
+        }
+        nodeDn[q] = float(dn);
+        return;
+    }
     const double *m = nodeMB + 12 * q;
     dbl4 g = t.geom[q];
     double X[3] = {g.x, g.y, g.z};
     float *o = nodeDC + 12 * q;
     float *ol = nodeDCl + 12 * q;
+    double dn = 0.0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double Mx = 0.0;
+        double Mx = 0.0, rowsum = 0.0;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            double d = m[3 * a + k] - (a == k ? 1.0 : 0.0);
-            o[3 * a + k] = float(d);
-            ol[3 * a + k] = float(d - double(float(d)));
+            double d = m[3 * a + k] - (a == k ? 1.0 : 0.0) - Dr[3 * a + k];
+            split_store(d, o + 3 * a + k, ol + 3 * a + k);
             Mx += d * X[k];
+            rowsum += fabs(d);
         }
-        double cval = Mx + m[9 + a];
-        o[9 + a] = float(cval);
-        ol[9 + a] = float(cval - double(float(cval)));
+        dn = fmax(dn, rowsum);
+        split_store(Mx + (m[9 + a] - br[a]), o + 9 + a, ol + 9 + a);
     }
+    nodeDn[q] = float(dn);
 }
 
 __global__ void k_to_float(int64_t n, const double *src, float *dst) {
@@ -322,12 +369,16 @@ void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, 
                                                         ptXA, ptDA);
 }
 
-void launch_mixed_nodal(int n, const dbl4 *ptXA, const double *ptMB, float *ptDM, float *ptDMl, cudaStream_t st) {
-    if (n > 0) k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, ptXA, ptMB, ptDM, ptDMl);
+void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
+                        float *ptDM, float *ptDMl, cudaStream_t st) {
+    if (n > 0 && t.nNodes > 0)
+        k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, t, nodeMB, ptXA, ptMB, ptDM, ptDMl);
 }
 
-void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, float *nodeDC, float *nodeDCl, cudaStream_t st) {
-    if (t.nNodes > 0) k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, nodeDC, nodeDCl);
+void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
+                        float *nodeDn, float *refDB, cudaStream_t st) {
+    if (t.nNodes > 0)
+        k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, ptMB, nodeDC, nodeDCl, nodeDn, refDB);
 }
 
 // Sort volume nodes by Morton code (set-up).  perm[k] = common index of the
