@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                     cnt.visited++;
                     dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
                 }
-                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, cnt.fallback);
+                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 if (__any_sync(kFull, dec == 1)) {
                     float w = 0.f;
                     if (dec == 1) {

@@ -10,7 +10,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/idwarp_gb300.h"
+#include "idwarp_gb300.h"
 #include "idw_host.hpp"
 #include "idw_kernels.h"
 

@@ -58,12 +58,8 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
         while (node < t.nNodes) {
             const int4 inf = ldgi4(&tf.nodes[node].info);
             const bool active = valid && node >= skip;
-            if (mp.slotStats && __any_sync(kFull, active)) {
-                if (inf.w)
-                    cnt.leafSlots += 32u * (inf.y - inf.x + 1);
-                else
-                    cnt.nodeSlots += 32u;
-            }
+            if (mp.slotStats && __any_sync(kFull, active) && counters && (threadIdx.x & 31) == 0)
+                atomicAdd(counters + (inf.w ? 4 : 5), (unsigned long long)(inf.w ? 32 * (inf.y - inf.x + 1) : 32));
             if (inf.w) {
                 bool leafPrecise = false;
                 if (active) {
@@ -138,8 +134,8 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                             precise_term<KIND>(x, 1e-15f, da.w, dl.w, pf.dm + 12 * i, pf.dml + 12 * i, law, Ls, LsLo,
                                                c1, mp.abH, mp.abL, sn, cn, sd, cd);
                         }
-                        cnt.precise += inf.y - inf.x + 1;
                     }
+                    warp_count(counters, 6, leafPrecise ? unsigned(inf.y - inf.x + 1) : 0u);
                 }
                 node = inf.z;
             } else {
@@ -150,7 +146,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                     cnt.visited++;
                     dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
                 }
-                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, cnt.fallback);
+                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 bool precise = false;
                 if (dec == 1) {
                     const float tt = fmaf(Ls, rs, LsLo * rs);
@@ -194,8 +190,8 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                         q[2].l += rl[2] - cl.z;
                         precise_term<KIND>(q, 0.f, cl.w, __ldg(&tf.nodes[node].aLo), af.dc + 12 * node,
                                            af.dcl + 12 * node, law, Ls, LsLo, c1, mp.abH, mp.abL, sn, cn, sd, cd);
-                        cnt.precise++;
                     }
+                    warp_count(counters, 6, precise ? 1u : 0u);
                 }
                 node = __any_sync(kFull, open) ? node + 1 : inf.z;
             }

@@ -7,19 +7,30 @@
 
 namespace idw {
 
-// Per-lane work counters (32-bit per lane; summed in 64 bits per warp).
+// Per-lane work counters of the frequent events (32-bit per lane; summed in
+// 64 bits per warp at the end).  Slots: dst[0] leaf pairs, dst[1] cluster
+// approximations, dst[2] visited nodes; the rare events (FP64 decision
+// fallbacks dst[3], diagnostic slot counts dst[4..5], double-float terms
+// dst[6]) go straight to memory with warp_count, which keeps them out of the
+// walk's registers.
 struct MixedCounters {
-    unsigned leafPairs = 0, approx = 0, visited = 0, fallback = 0, leafSlots = 0, nodeSlots = 0, precise = 0;
+    unsigned leafPairs = 0, approx = 0, visited = 0;
     __device__ void flush(unsigned long long *dst) {
         if (!dst) return;
-        const unsigned long long v[7] = {leafPairs, approx, visited, fallback, leafSlots, nodeSlots, precise};
+        const unsigned long long v[3] = {leafPairs, approx, visited};
 #pragma unroll
-        for (int k = 0; k < 7; ++k) {
+        for (int k = 0; k < 3; ++k) {
             const unsigned long long s = warp_sum(v[k]);
             if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst + k, s);
         }
     }
 };
+
+// Warp-wide count into dst[k]; every lane of a converged warp must call it.
+__device__ __forceinline__ void warp_count(unsigned long long *dst, int k, unsigned v) {
+    const unsigned s = __reduce_add_sync(kFull, v);
+    if (dst && s && (threadIdx.x & 31) == 0) atomicAdd(dst + k, (unsigned long long)s);
+}
 
 // Law kinds: 0 = exponents (3,5); 1 = other integer exponents; 2 = real.
 template <int KIND>
@@ -292,15 +303,17 @@ __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const floa
 // Re-take undecided decisions with the FP64 rule (all lanes of the warp call
 // this; the FP64 work runs only when some lane needs it).
 __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const VolumeDev &v, int64_t g, int node,
-                                         const float *rh, const float *rl, double errTol, unsigned &fallback) {
+                                         const float *rh, const float *rl, double errTol,
+                                         unsigned long long *counters) {
     if (__any_sync(kFull, dec == 2)) {
-        if (dec == 2) {
+        const bool redo = dec == 2;
+        if (redo) {
             const int vi = v.perm[g];
             double r[3] = {double(rh[0]) + double(rl[0]), double(rh[1]) + double(rl[1]), double(rh[2]) + double(rl[2])};
             double dist64;
             dec = decide64(t.geom[node], t.err + kNerr * node, r, errTol * v.den0[vi], dist64);
-            fallback++;
         }
+        warp_count(counters, 3, redo ? 1u : 0u);
     }
     return dec;
 }

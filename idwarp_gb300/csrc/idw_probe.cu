@@ -2,7 +2,7 @@
 // Eight independent FMA chains per thread, enough blocks to fill every SM.
 #include <cuda_runtime.h>
 
-#include "../../include/idwarp_gb300.h"
+#include "idwarp_gb300.h"
 
 namespace {
 
