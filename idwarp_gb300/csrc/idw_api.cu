@@ -621,7 +621,7 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = c->opt.diagnostics & 1;
-    // terms whose weight share x lever arm exceeds mixedGate*Ldef are summed in double-float
+    // terms whose weight x (motion + lever arm) exceeds mixedGate*Ldef*den0 are summed in double-float
     k.precGate = c->opt.mixedGate * c->Ldef0 * c->opt.LdefFact;
     PointsDev p;
     p.xa = c->ptXA.p;

@@ -69,6 +69,7 @@ struct MixedParams {
     int slotStats;  // count warp-level lane slots (diagnostics)
     float LdefLo, abH, abL, precGate;
     double bExp;
+    float bExpF;
 };
 
 struct NodeAggF {

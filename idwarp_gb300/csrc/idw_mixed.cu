@@ -44,6 +44,12 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
     const float c1 = mp.intExp ? pow2f(s * mp.dExp) : exp2f(float(s) * mp.dExpF);
     const float ab = mp.abH, abl = mp.abL;
     const float tauf = mp.errTolF * den0f;
+    // precision gate: a term whose FP32 rounding, w (|S'| + |D'| |r - X|) u,
+    // could exceed mixedGate * Ldef * u of the final denominator is summed in
+    // double-float.  The final (scaled) denominator is estimated by den0 sigma^b.
+    const float gexp = float(s) * mp.bExpF;
+    const float gexpi = floorf(gexp);
+    const float gv = mp.precGate * ldexpf(den0f, int(gexpi)) * exp2f(gexp - gexpi);
     // running sums over the mirrors (sum = S + C per component), kept in shared
     // memory between mirror passes to free registers for the walk
     __shared__ float4 mirS[128], mirC[128];
@@ -94,15 +100,11 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                         pn2 = fmaf(w, S2, pn2);
                         pd += w;
                     }
-                    // a leaf carrying a large weight share at a long lever arm is
+                    // a leaf carrying a large weight at a long lever arm is
                     // re-summed in double-float (same gate as cluster terms)
                     const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) +
                                        pd * __ldg(af.dn + node) * (fabsf(h0) + fabsf(h1) + fabsf(h2));
-                    const float ldev = sd > 0.f ? lmag * sd + fabsf(fmaf(pn0, sd, -pd * sn[0])) +
-                                                      fabsf(fmaf(pn1, sd, -pd * sn[1])) +
-                                                      fabsf(fmaf(pn2, sd, -pd * sn[2]))
-                                                : lmag;
-                    leafPrecise = KIND != 2 && ldev > mp.precGate * (sd > 0.f ? sd : 1.f);
+                    leafPrecise = KIND != 2 && lmag > gv;
                     if (!leafPrecise) {
                         kahan_add(sn[0], cn[0], pn0);
                         kahan_add(sn[1], cn[1], pn1);
@@ -156,17 +158,11 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                     const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
                     const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
                     const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
-                    // A far cluster whose share of the weight times its lever arm
-                    // is large enough for FP32 rounding to show in Xv is
-                    // re-evaluated in double-float below.
-                    // FP32 rounding error of this term in Xv ~ u * w (|S| + |S - num/den|) / den:
-                    // the size of S plus its deviation from the running average
+                    // a far cluster with a large weight at a long lever arm is
+                    // re-evaluated in double-float below
                     const float mag = fabsf(S0) + fabsf(S1) + fabsf(S2) +
                                       __ldg(af.dn + node) * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
-                    const float dev = sd > 0.f ? mag * sd + fabsf(fmaf(S0, sd, -sn[0])) +
-                                                     fabsf(fmaf(S1, sd, -sn[1])) + fabsf(fmaf(S2, sd, -sn[2]))
-                                               : mag;
-                    precise = KIND != 2 && w * dev > mp.precGate * (sd > 0.f ? sd : 1.f);
+                    precise = KIND != 2 && w * mag > gv;
                     if (!precise) {
                         kahan_add(sn[0], cn[0], w * S0);
                         kahan_add(sn[1], cn[1], w * S1);
@@ -314,6 +310,7 @@ MixedParams make_mixed_params(const EvalConsts &k) {
     mp.dExpF = float(k.law.bExp - k.law.aExp);
     mp.slotStats = k.slotStats;
     mp.bExp = k.law.bExp;
+    mp.bExpF = float(k.law.bExp);
     return mp;
 }
 
