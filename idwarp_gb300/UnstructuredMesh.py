@@ -70,6 +70,7 @@ class USMesh(BaseSolver):
         self.nSurf = 0
         self.nVol = 0
         self.solverMeshDOF = None
+        self._surfVersion = 0
         self._setMeshOptions()
         self.fileType = self.getOption("fileType")
         fileName = self.getOption("gridFile")
@@ -157,6 +158,7 @@ class USMesh(BaseSolver):
         ptr, where = _lib.vptr(coordinates)
         self._chk(self.lib.idw_set_surface_coordinates(self.ctx, ptr, 3 * self.nSurf, where),
                     "setSurfaceCoordinates")
+        self._surfVersion += 1
 
     def setExternalMeshIndices(self, ind):
         """Set the 0-based DOF indices of the solver grid into the common grid."""
@@ -274,8 +276,28 @@ class USMesh(BaseSolver):
         self._chk(self.lib.idw_warp_deriv(self.ctx, ptr, n, where), "warpDeriv")
 
     def warpDerivFwd(self, dXs, solverVec=True):
-        """Forward-mode product dXv = (dXv/dXs) dXs (idwarp/UnstructuredMesh.py:428-459)."""
-        raise Error("warpDerivFwd is not available in this build of idwarp_gb300.")
+        """Forward-mode product dXv = (dXv/dXs) dXs (idwarp/UnstructuredMesh.py:428-459).
+
+        dXs has the shape of getSurfaceCoordinates(); returns dXv in solver
+        ordering (solverVec=True) or warp ordering, flat.  Like the reference,
+        the mesh is warped first."""
+        dXs = np.ascontiguousarray(np.asarray(dXs, dtype=np.float64).ravel())
+        if dXs.size != 3 * self.nSurf:
+            raise Error("dXs has %d entries, expected %d" % (dXs.size, 3 * self.nSurf))
+        dXvWarp = np.zeros(3 * self.nVol, self.dtype)
+        self.warpMesh()
+        self._chk(self.lib.idw_warp_deriv_fwd(self.ctx, C.c_void_p(dXs.ctypes.data), dXs.size,
+                                              C.c_void_p(dXvWarp.ctypes.data), dXvWarp.size, _lib.IDW_HOST),
+                  "warpDerivFwd")
+        if solverVec:
+            if self.solverMeshDOF is None:
+                raise Error("setExternalMeshIndices() must be called before warpDerivFwd(solverVec=True).")
+            dXv = np.zeros(self.solverMeshDOF, self.dtype)
+            self._chk(self.lib.idw_warp_to_solver_grid(self.ctx, C.c_void_p(dXvWarp.ctypes.data), dXvWarp.size,
+                                                       C.c_void_p(dXv.ctypes.data), dXv.size, _lib.IDW_HOST),
+                      "warp_to_solver_grid")
+            return dXv
+        return dXvWarp
 
     def verifyWarpDeriv(self, dXv=None, solverVec=True, dofStart=0, dofEnd=10, h=1e-6, randomSeed=314):
         """Compare warpDeriv with central differences on a few surface DOFs (src/warp/verifyWarpDeriv.F90)."""

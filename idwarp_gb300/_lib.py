@@ -82,6 +82,7 @@ _SIGS = {
     "idw_warp_deriv": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_dxs": [_VP, _VP, C.c_int64, C.c_int],
     "idw_warp_deriv_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
+    "idw_warp_deriv_fwd": [_VP, _VP, C.c_int64, _VP, C.c_int64, C.c_int],
     "idw_get_denominator0": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_denominator": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_stats": [_VP, C.POINTER(idw_stats)],

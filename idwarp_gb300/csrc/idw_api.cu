@@ -70,6 +70,10 @@ struct Ctx {
     DevBuf<NodeRecF> nodeRec;
     DevBuf<float4> ptDA, ptDL;
     DevBuf<float4> recHi, recLo, acc;  // per-volume-node walk records and accumulators
+    DevBuf<float> gden;                // per node: scaled denominator of a mixed walk (precision gate)
+    bool gdenValid = false;
+    double gdenLdefFact = 0.0, gdenAlpha = 0.0;
+    int gdenMode = -1;
     DevBuf<float> ptDM, ptDMl, nodeDC, nodeDCl, nodeDn, refDB;
     // adjoint
     DevBuf<double> ptAdj, nodeAdj, xub, dxs;
@@ -572,6 +576,8 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->recHi.alloc(size_t(c->sym.nLoop) * c->nVol));
     CKA(c->recLo.alloc(size_t(c->sym.nLoop) * c->nVol));
     CKA(c->acc.alloc(2 * size_t(c->nVol)));
+    CKA(c->gden.alloc(size_t(c->nVol)));
+    c->gdenValid = false;
     launch_walk_records(vol_dev(c), c->sym, c->optInit.bExp, c->recHi.p, c->recLo.p, st);
     e = check_launch(c, "walk records");
     if (e) return e;
@@ -612,6 +618,29 @@ int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int whe
     return copy_out(c, coords, c->xs.p, size_t(cdof), where);
 }
 
+// The mixed walk's precision gate wants each node's final denominator, which
+// depends on Xu0 and the weight law only (not on the surface coordinates):
+// one walk that keeps only the denominators, run once per law.
+static int ensure_gate_den(Ctx *c, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, const WalkRecF &rec,
+                           const EvalConsts &k, int exact) {
+    if (c->gdenValid && c->gdenLdefFact == c->opt.LdefFact && c->gdenAlpha == c->opt.alpha &&
+        c->gdenMode == c->opt.evalMode)
+        return IDW_OK;
+    WalkOut none;
+    EvalConsts k0 = k;
+    k0.precGate = 3.0e38;  // FP32 terms only: a gate needs no more
+    launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), rec, k0, exact, c->acc.p, none, c->stream);
+    launch_gate_den(c->nVol, c->acc.p, c->gden.p, c->stream);
+    int rc = check_launch(c, "gate denominators");
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+    c->gdenValid = true;
+    c->gdenLdefFact = c->opt.LdefFact;
+    c->gdenAlpha = c->opt.alpha;
+    c->gdenMode = c->opt.evalMode;
+    return IDW_OK;
+}
+
 static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
     int rc = refresh_nodal(c);
@@ -649,6 +678,10 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
+        int rc2 = ensure_gate_den(c, tf, pf, af, rec, k, exact);
+        if (rc2) return rc2;
+        rec.gden = c->gden.p;
+        CK(cudaEventRecord(c->ev0, c->stream));
         launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), rec, k, exact, c->acc.p, o, c->stream);
     } else {
         launch_walk_fp64(tree_dev(c), p, vol_dev(c), c->nodeMB.p, k, exact, c->nUnique, o, c->stream);
@@ -661,9 +694,9 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
 static int read_counters(Ctx *c) {
     unsigned long long h[8];
     CK(cudaMemcpyAsync(h, c->counters.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     c->stats.warpLeafSlots = int64_t(h[4]);
     c->stats.warpNodeSlots = int64_t(h[5]);
-    CK(cudaStreamSynchronize(c->stream));
     c->stats.leafPairs = int64_t(h[0]);
     c->stats.approx = int64_t(h[1]);
     c->stats.visited = int64_t(h[2]);
@@ -917,9 +950,132 @@ __global__ void k_scatter_add_dof(int64_t n, const int *ind, const double *src, 
     int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k < n) atomicAdd(dst + ind[k], src[k]);
 }
+// max |v| (non-negative doubles order like their bit patterns)
+__global__ void k_absmax(int64_t n, const double *v, unsigned long long *out) {
+    int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double a = k < n ? fabs(v[k]) : 0.0;
+    if (!(a <= 1.7976931348623157e308)) a = 0.0;  // non-finite entries are rejected by the caller
+    unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long q = __shfl_down_sync(0xffffffffu, b, o);
+        b = q > b ? q : b;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out, b);
+}
+
+// warpDerivFwd (src/warp/warpDerivFwd.F90:58-97): Xvd = sum w (Md r + bd) / den.
+int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
+    const int n = c->nUnique, nn = c->nNodes;
+    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
+    const int mixed = c->opt.precision == IDW_PREC_MIXED;
+    DevBuf<double> xud, ptMBd, nodeMBd;
+    CKA(xud.alloc(3 * size_t(n)));
+    CKA(ptMBd.alloc(12 * size_t(n)));
+    CKA(nodeMBd.alloc(12 * size_t(nn)));
+    // Xu, Xud = Xs, Xsd at the first caller occurrence of each unique point
+    launch_gather_xu(n, c->xuInd.p, c->xs.p, c->xu.p, c->stream);
+    launch_gather_xu(n, c->xuInd.p, xsdDev, xud.p, c->stream);
+    // (Md + I, bd): the forward walk with S = (Md + I) r + bd - r = Md r + bd
+    launch_nodal_d(surf_dev(c), c->xu.p, xud.p, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p,
+                   c->opt.useRotations, 1, ptMBd.p, c->stream);
+    launch_set_data(tree_dev(c), ptMBd.p, nodeMBd.p, c->stream);
+    int rc = check_launch(c, "tangent nodal properties");
+    if (rc) return rc;
+    EvalConsts k;
+    k.law = make_law(c);
+    k.errTol = c->opt.errTol;
+    k.sym = c->sym;
+    k.slotStats = 0;
+    k.precGate = 0.0;
+    WalkOut o;
+    o.xv = xvdDev;
+    o.counters = c->counters.p;
+    o.tangent = 1;
+    o.denIn = c->den.p;
+    CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+    if (mixed) {
+        // the gate scales with the size of the tangent instead of Ldef
+        CK(cudaMemsetAsync(c->counters.p + 7, 0, sizeof(unsigned long long), c->stream));
+        const int64_t nd = 3 * int64_t(n);
+        k_absmax<<<int((nd + 255) / 256), 256, 0, c->stream>>>(nd, xud.p, c->counters.p + 7);
+        unsigned long long bits = 0;
+        CK(cudaMemcpyAsync(&bits, c->counters.p + 7, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        double scale;
+        std::memcpy(&scale, &bits, sizeof(scale));
+        k.precGate = c->opt.mixedGate * scale;
+        CK(cudaMemsetAsync(c->counters.p + 7, 0, sizeof(unsigned long long), c->stream));
+        // the FP32 walk arrays now describe the tangent; the next warp rebuilds them
+        launch_mixed_nodal(n, tree_dev(c), nodeMBd.p, c->ptXA.p, ptMBd.p, c->ptDM.p, c->ptDMl.p, c->stream);
+        launch_mixed_nodes(tree_dev(c), nodeMBd.p, ptMBd.p, c->nodeDC.p, c->nodeDCl.p, c->nodeDn.p, c->refDB.p,
+                           c->stream);
+        c->nodalValid = false;
+        TreeDevF tf;
+        tf.nodes = c->nodeRec.p;
+        PointsDevF pf;
+        pf.da = c->ptDA.p;
+        pf.dl = c->ptDL.p;
+        pf.dm = c->ptDM.p;
+        pf.dml = c->ptDMl.p;
+        NodeAggF af;
+        af.dc = c->nodeDC.p;
+        af.dcl = c->nodeDCl.p;
+        af.dn = c->nodeDn.p;
+        af.ref = c->refDB.p;
+        WalkRecF rec;
+        rec.hi = c->recHi.p;
+        rec.lo = c->recLo.p;
+        rec.gden = c->gdenValid ? c->gden.p : nullptr;
+        CK(cudaEventRecord(c->ev0, c->stream));
+        launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), rec, k, exact, c->acc.p, o, c->stream);
+    } else {
+        PointsDev p;
+        p.xa = c->ptXA.p;
+        p.mb = ptMBd.p;
+        CK(cudaEventRecord(c->ev0, c->stream));
+        launch_walk_fp64(tree_dev(c), p, vol_dev(c), nodeMBd.p, k, exact, n, o, c->stream);
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    c->eventsRecorded = true;
+    rc = check_launch(c, "tangent walk");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
 }  // namespace
 
 extern "C" {
+
+int idw_warp_deriv_fwd(void *ctx, const double *dxs, int64_t cdof, double *dxv, int64_t ndof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDerivFwd");
+    if (!dxs || !dxv) return fail(c, IDW_ERR_ARG, "null dXs or dXv");
+    if (cdof != 3 * int64_t(c->nPts))
+        return fail(c, IDW_ERR_ARG, "dXs has %lld entries, expected %lld", (long long)cdof,
+                    (long long)(3 * int64_t(c->nPts)));
+    if (ndof != 3 * c->nVol)
+        return fail(c, IDW_ERR_ARG, "dXv has %lld entries, expected %lld", (long long)ndof, (long long)(3 * c->nVol));
+    if (where != IDW_DEVICE && !all_finite(dxs, size_t(cdof)))
+        return fail(c, IDW_ERR_NONFINITE, "non-finite dXs");
+    CK(cudaSetDevice(c->device));
+    const double *in = dxs;
+    double *out = dxv;
+    DevBuf<double> tin, tout;
+    if (where != IDW_DEVICE) {
+        CKA(tin.alloc(size_t(cdof)));
+        CKA(tout.alloc(size_t(ndof)));
+        int rc = copy_in(c, tin.p, dxs, size_t(cdof), IDW_HOST);
+        if (rc) return rc;
+        in = tin.p;
+        out = tout.p;
+    }
+    int rc = run_deriv_fwd(c, in, out);
+    if (rc) return rc;
+    if (where != IDW_DEVICE) return copy_out(c, dxv, tout.p, size_t(ndof), IDW_HOST);
+    return IDW_OK;
+}
 
 int idw_warp_to_solver_grid(void *ctx, const double *warp, int64_t wdof, double *solver, int64_t sdof, int where) {
     Ctx *c = static_cast<Ctx *>(ctx);

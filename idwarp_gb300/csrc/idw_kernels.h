@@ -57,6 +57,7 @@ struct PointsDevF {
 struct WalkRecF {
     const float4 *hi;  // mirrored point, high part; denominator estimate (FP32)
     const float4 *lo;  // mirrored point, low part; scale exponent s (int bits)
+    const float *gden = nullptr;  // per node: the walk's own scaled denominator (precision gate), or null
 };
 
 struct MixedParams {
@@ -87,9 +88,12 @@ struct VolumeDev {
 };
 
 struct WalkOut {
-    double *xv;            // (nVol,3) or nullptr
-    double *den;           // (nVol) true-unit denominators or nullptr
-    unsigned long long *counters;  // leafPairs, approx, visited, fp64Fallback
+    double *xv = nullptr;            // (nVol,3) or nullptr
+    double *den = nullptr;           // (nVol) true-unit denominators or nullptr
+    unsigned long long *counters = nullptr;  // leafPairs, approx, visited, fp64Fallback, ...
+    // tangent mode (warpDerivFwd): xv receives num/denIn, without Xv0
+    int tangent = 0;
+    const double *denIn = nullptr;
 };
 
 struct EvalConsts {
@@ -113,6 +117,10 @@ void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const
                     const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
                     cudaStream_t st);
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st);
+// Tangent nodal properties: (Md [+ I], bd) per point, 12 doubles (M row-major, b).
+void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,
+                    const double *Ai, const int *isCorner, int useRotations, int plusIdentity, double *ptMBd,
+                    cudaStream_t st);
 
 // Set-up kernels (idw_setup.cu)
 void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err,
@@ -137,6 +145,8 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
                        const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
                        const WalkOut &o, cudaStream_t st);
 void launch_to_float(int64_t n, const double *src, float *dst, cudaStream_t st);
+// Per node (Morton order): the scaled denominator of the last mixed walk (acc).
+void launch_gate_den(int64_t nVol, const float4 *acc, float *gden, cudaStream_t st);
 int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,
                              int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,
                              double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,

@@ -46,10 +46,18 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
     const float tauf = mp.errTolF * den0f;
     // precision gate: a term whose FP32 rounding, w (|S'| + |D'| |r - X|) u,
     // could exceed mixedGate * Ldef * u of the final denominator is summed in
-    // double-float.  The final (scaled) denominator is estimated by den0 sigma^b.
-    const float gexp = float(s) * mp.bExpF;
-    const float gexpi = floorf(gexp);
-    const float gv = mp.precGate * ldexpf(den0f, int(gexpi)) * exp2f(gexp - gexpi);
+    // double-float.  The final (scaled) denominator is the walk's own from an
+    // earlier pass (it depends on Xu0 and the weight law only), else the
+    // estimate den0 sigma^b (which overestimates it on the wall, where den0's
+    // softening 1e-16 is below the walk's 1e-15).
+    float gv;
+    if (rec.gden) {
+        gv = mp.precGate * rec.gden[g];
+    } else {
+        const float gexp = float(s) * mp.bExpF;
+        const float gexpi = floorf(gexp);
+        gv = mp.precGate * ldexpf(den0f, int(gexpi)) * exp2f(gexp - gexpi);
+    }
     // running sums over the mirrors (sum = S + C per component), kept in shared
     // memory between mirror passes to free registers for the walk
     __shared__ float4 mirS[128], mirC[128];
@@ -240,7 +248,8 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
 
 // Normalisation and add-back in FP64: Xv = Xv0 + num/den, and the true-unit
 // denominator den/sigma^b for the derivative.
-__global__ void k_finalize_mixed(VolumeDev v, WalkRecF rec, const float4 *acc, double bExp, double *xv, double *den) {
+__global__ void k_finalize_mixed(VolumeDev v, WalkRecF rec, const float4 *acc, double bExp, int tangent, double *xv,
+                                 double *den) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (gid >= v.nVol) return;
     const int vi = v.perm[gid];
@@ -249,9 +258,12 @@ __global__ void k_finalize_mixed(VolumeDev v, WalkRecF rec, const float4 *acc, d
     const double D = double(a.w) + double(c.w);
     const double oden = 1.0 / D;
     if (xv) {
-        xv[3 * vi + 0] = v.xv0[3 * vi + 0] + N0 * oden;
-        xv[3 * vi + 1] = v.xv0[3 * vi + 1] + N1 * oden;
-        xv[3 * vi + 2] = v.xv0[3 * vi + 2] + N2 * oden;
+        // tangent mode: the derivative numerator over the (same) denominator
+        const double b0 = tangent ? 0.0 : v.xv0[3 * vi + 0], b1 = tangent ? 0.0 : v.xv0[3 * vi + 1],
+                     b2 = tangent ? 0.0 : v.xv0[3 * vi + 2];
+        xv[3 * vi + 0] = b0 + N0 * oden;
+        xv[3 * vi + 1] = b1 + N1 * oden;
+        xv[3 * vi + 2] = b2 + N2 * oden;
     }
     if (den) {
         const int s = __float_as_int(rec.lo[gid].w);
@@ -284,9 +296,19 @@ __global__ void k_walk_records(VolumeDev v, SymPlanes sym, double bExp, float4 *
     }
 }
 
+__global__ void k_gate_den(int64_t nVol, const float4 *acc, float *gden) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gid >= nVol) return;
+    gden[gid] = acc[2 * gid].w + acc[2 * gid + 1].w;
+}
+
 inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 
 }  // namespace
+
+void launch_gate_den(int64_t nVol, const float4 *acc, float *gden, cudaStream_t st) {
+    if (nVol > 0) k_gate_den<<<blocks(nVol, 256), 256, 0, st>>>(nVol, acc, gden);
+}
 
 MixedParams make_mixed_params(const EvalConsts &k) {
     MixedParams mp;
@@ -335,7 +357,8 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
         Law32<2> law{0, 0, float(k.law.aExp), float(k.law.bExp)};
         k_walk_mixed<2><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
     }
-    k_finalize_mixed<<<blocks(v.nVol, 256), 256, 0, st>>>(v, rec, acc, k.law.bExp, o.xv, o.den);
+    k_finalize_mixed<<<blocks(v.nVol, 256), 256, 0, st>>>(v, rec, acc, k.law.bExp, o.tangent, o.xv,
+                                                          o.tangent ? nullptr : o.den);
 }
 
 }  // namespace idw

@@ -6,6 +6,9 @@
 //            setData                  src/modules/kd_tree.F90:595-617
 //   reverse  COMPUTENODALPROPERTIES_B src/modules/kd_tree.F90:1057-1162
 //            setData_b                src/modules/kd_tree.F90:1033-1051
+//   tangent  COMPUTENODALPROPERTIES_D src/modules/kd_tree.F90:1250-1356
+//            GETELEMENTPROPS_D        src/adjoint/outputForward/getElementProps_d.f90
+//            GETROTATIONMATRIX3D_D    src/adjoint/outputForward/vectorUtils_d.f90:7-119
 // The reverse kernels recompute the forward intermediates of each node in
 // registers instead of replaying a tape.
 #include "idw_common.cuh"
@@ -437,6 +440,161 @@ __global__ void k_scatter_dxs(int n, const int *xuInd, const double *Xub, double
     dXs[3 * j + 2] = Xub[3 * i + 2];
 }
 
+// ---- tangent (forward-mode) nodal properties ----
+
+// element_props and its directional derivative along Xud.
+__device__ void element_props_d(const double *Xu, const double *Xud, const int *conn, int np, double &area,
+                                double &aread, double *normal, double *normald) {
+    double c[3] = {0, 0, 0}, cd[3] = {0, 0, 0};
+    for (int k = 0; k < np; ++k) {
+        const double *p = Xu + 3 * conn[k];
+        const double *pd = Xud + 3 * conn[k];
+        for (int a = 0; a < 3; ++a) {
+            c[a] += p[a];
+            cd[a] += pd[a];
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        c[a] /= double(np);
+        cd[a] /= double(np);
+    }
+    double nrm[3] = {0, 0, 0}, nrmd[3] = {0, 0, 0};
+    double ar = 0, ard = 0;
+    for (int k = 0; k < np; ++k) {
+        const int j = k < np - 1 ? k + 1 : 0;
+        const double *pi = Xu + 3 * conn[k], *pj = Xu + 3 * conn[j];
+        const double *pid = Xud + 3 * conn[k], *pjd = Xud + 3 * conn[j];
+        double a[3], b[3], ad[3], bd[3];
+        for (int q = 0; q < 3; ++q) {
+            a[q] = pi[q] - c[q];
+            b[q] = pj[q] - c[q];
+            ad[q] = pid[q] - cd[q];
+            bd[q] = pjd[q] - cd[q];
+        }
+        double cr[3], t1[3], t2[3];
+        cross3(a, b, cr);
+        cross3(ad, b, t1);
+        cross3(a, bd, t2);
+        const double crd[3] = {t1[0] + t2[0], t1[1] + t2[1], t1[2] + t2[2]};
+        const double cn = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2] + 1e-15);
+        const double cnd = (cr[0] * crd[0] + cr[1] * crd[1] + cr[2] * crd[2]) / cn;
+        ar += 0.5 * cn;
+        ard += 0.5 * cnd;
+        for (int q = 0; q < 3; ++q) {
+            nrm[q] += cr[q] / cn;
+            nrmd[q] += (crd[q] - cr[q] * cnd / cn) / cn;
+        }
+    }
+    const double m = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+    const double md = (nrm[0] * nrmd[0] + nrm[1] * nrmd[1] + nrm[2] * nrmd[2]) / m;
+    for (int q = 0; q < 3; ++q) {
+        normal[q] = nrm[q] / m;
+        normald[q] = (nrmd[q] - nrm[q] * md / m) / m;
+    }
+    area = ar;
+    aread = ard;
+}
+
+// rotation_matrix and its derivative along v2d (v1 = normals0 is fixed).
+// The derivative is zero when the axis is degenerate, and the angle carries
+// none when the acos argument was clamped or is +-1, as GETROTATIONMATRIX3D_D.
+__device__ void rotation_matrix_d(const double *v1, const double *v2, const double *v2d, double *M, double *Md) {
+    const double mag1 = mag_eps(v1), mag2 = mag_eps(v2);
+    const double mag2d = (v2[0] * v2d[0] + v2[1] * v2d[1] + v2[2] * v2d[2]) / mag2;
+    double ax[3], axd[3];
+    cross3(v1, v2, ax);
+    cross3(v1, v2d, axd);
+    const double axm = mag_eps(ax);
+    double s, omc, sd, omcd;
+    if (axm < kRotTol) {
+        ax[0] = 1.0;
+        ax[1] = ax[2] = 0.0;
+        axd[0] = axd[1] = axd[2] = 0.0;
+        s = omc = sd = omcd = 0.0;
+    } else {
+        const double axmd = (ax[0] * axd[0] + ax[1] * axd[1] + ax[2] * axd[2]) / axm;
+        for (int q = 0; q < 3; ++q) {
+            axd[q] = (axd[q] - ax[q] * axmd / axm) / axm;
+            ax[q] /= axm;
+        }
+        double d = 0.0, dd = 0.0;
+        for (int q = 0; q < 3; ++q) {
+            const double vv1 = v1[q] / mag1;
+            d += vv1 * (v2[q] / mag2);
+            dd += vv1 * ((v2d[q] - v2[q] * mag2d / mag2) / mag2);
+        }
+        double arg = d, argd = dd;
+        if (!(1.0 > d)) {
+            arg = 1.0;
+            argd = 0.0;
+        }
+        const double angd = (arg == 1.0 || arg == -1.0) ? 0.0 : -(argd / sqrt(1.0 - arg * arg));
+        const double ang = acos(arg);
+        s = sin(ang);
+        omc = 1.0 - cos(ang);
+        sd = cos(ang) * angd;
+        omcd = s * angd;
+    }
+    const double A[9] = {0.0, -ax[2], ax[1], ax[2], 0.0, -ax[0], -ax[1], ax[0], 0.0};
+    const double Ad[9] = {0.0, -axd[2], axd[1], axd[2], 0.0, -axd[0], -axd[1], axd[0], 0.0};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double C = 0.0, Cd = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                C += A[3 * i + k] * A[3 * k + j];
+                Cd += Ad[3 * i + k] * A[3 * k + j] + A[3 * i + k] * Ad[3 * k + j];
+            }
+            M[3 * i + j] = (i == j ? 1.0 : 0.0) + s * A[3 * i + j] + omc * C;
+            Md[3 * i + j] = sd * A[3 * i + j] + s * Ad[3 * i + j] + omcd * C + omc * Cd;
+        }
+}
+
+__global__ void k_nodal_d(SurfaceDev s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,
+                          const double *Ai, const int *isCorner, int useRotations, int plusIdentity, double *ptMBd) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s.n) return;
+    double Md[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double bd[3] = {0, 0, 0};
+    // nodes without faces keep M = I, b = 0 and carry no derivative
+    if (Ai[i] != 0.0) {
+        if (useRotations && !isCorner[i]) {
+            double sa = 0.0, sad = 0.0, sn[3] = {0, 0, 0}, snd[3] = {0, 0, 0};
+            for (int e = s.n2ePtr[i]; e < s.n2ePtr[i + 1]; ++e) {
+                const int f = s.n2e[e];
+                const int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
+                double area, aread, fn[3], fnd[3];
+                element_props_d(Xu, Xud, s.faceConn + f0, np, area, aread, fn, fnd);
+                const double dA = area / double(np), dAd = aread / double(np);
+                sa += dA;
+                sad += dAd;
+                for (int q = 0; q < 3; ++q) {
+                    sn[q] += dA * fn[q];
+                    snd[q] += dAd * fn[q] + dA * fnd[q];
+                }
+            }
+            double nrm[3], nrmd[3], M[9];
+            for (int q = 0; q < 3; ++q) {
+                nrm[q] = sn[q] / sa;
+                nrmd[q] = (snd[q] * sa - sn[q] * sad) / (sa * sa);
+            }
+            rotation_matrix_d(normals0 + 3 * i, nrm, nrmd, M, Md);
+        }
+        const dbl4 q = xa[i];
+        const double x0[3] = {q.x, q.y, q.z};
+        for (int a = 0; a < 3; ++a)
+            bd[a] = Xud[3 * i + a] - (Md[3 * a] * x0[0] + Md[3 * a + 1] * x0[1] + Md[3 * a + 2] * x0[2]);
+    }
+    double *o = ptMBd + 12 * i;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) o[q] = Md[q] + ((plusIdentity && (q % 4 == 0)) ? 1.0 : 0.0);
+    o[9] = bd[0];
+    o[10] = bd[1];
+    o[11] = bd[2];
+}
+
 inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 
 }  // namespace
@@ -468,6 +626,13 @@ void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const
     if (s.n > 0)
         k_nodal_b<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, isCorner, useRotations, ptAdj, relative,
                                                     Xub);
+}
+void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,
+                    const double *Ai, const int *isCorner, int useRotations, int plusIdentity, double *ptMBd,
+                    cudaStream_t st) {
+    if (s.n > 0)
+        k_nodal_d<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, Xud, xa, normals0, Ai, isCorner, useRotations,
+                                                    plusIdentity, ptMBd);
 }
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st) {
     if (n > 0) k_scatter_dxs<<<blocks(n, 256), 256, 0, st>>>(n, xuInd, Xub, dXs);

@@ -2,6 +2,10 @@
 //   fast walk   evalNode / evalNodeApprox     src/modules/kd_tree.F90:619-662, 692-713
 //   exact       evalNodeExact (on the root)   src/modules/kd_tree.F90:664-690
 //   driver      warpMesh                      src/warp/warpMesh.F90:37-70
+//   tangent     evalNode_d / evalNodeExact_d / evalNodeApprox_d  kd_tree.F90:1164-1236,
+//               driven as warpDerivFwd        src/warp/warpDerivFwd.F90:58-97
+//               (the walk is the forward one with (M, b) replaced by
+//               (Md + I, bd), so that S = Md r + bd)
 //   adjoint     evalNode_b / evalNodeExact_b / evalNodeApprox_b  kd_tree.F90:942-1031,
 //               driven as warpDeriv           src/warp/warpDeriv.F90:71-88
 //
@@ -132,13 +136,22 @@ __global__ void __launch_bounds__(128) k_walk64(TreeDev t, PointsDev p, VolumeDe
         denom += den;
     }
     if (valid) {
-        double oden = 1.0 / denom;
-        if (o.xv) {
-            o.xv[3 * vi + 0] = x0[0] + numer[0] * oden;
-            o.xv[3 * vi + 1] = x0[1] + numer[1] * oden;
-            o.xv[3 * vi + 2] = x0[2] + numer[2] * oden;
+        if (o.tangent) {
+            // warpDerivFwd.F90:91-97: the derivative numerator over the last
+            // warpMesh's denominator
+            const double oden = 1.0 / o.denIn[vi];
+            o.xv[3 * vi + 0] = numer[0] * oden;
+            o.xv[3 * vi + 1] = numer[1] * oden;
+            o.xv[3 * vi + 2] = numer[2] * oden;
+        } else {
+            double oden = 1.0 / denom;
+            if (o.xv) {
+                o.xv[3 * vi + 0] = x0[0] + numer[0] * oden;
+                o.xv[3 * vi + 1] = x0[1] + numer[1] * oden;
+                o.xv[3 * vi + 2] = x0[2] + numer[2] * oden;
+            }
+            if (o.den) o.den[vi] = denom;
         }
-        if (o.den) o.den[vi] = denom;
     }
     cnt.flush(o.counters);
 }

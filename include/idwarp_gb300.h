@@ -178,6 +178,14 @@ int idw_get_dxs(void *ctx, double *out, int64_t ndof, int where);
  * nseeds stacked (nvol,3) seeds, dxs receives nseeds stacked (npts,3). */
 int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *dxs, int where);
 
+/* Forward-mode (tangent) product dXv = (dXv/dXs) dXs.  Replaces the f2py
+ * entry warpderivfwd(xsdot, outvec) (src/f2py/libidwarp.pyf:107-112;
+ * src/warp/warpDerivFwd.F90:1-111): dxs (npts,3) in the caller's surface
+ * order, dxv (nvol,3) in warp (common) order, both on the host or both on
+ * the device (where).  Needs a prior idw_warp_mesh; the derivative numerator
+ * is divided by that warp's denominator. */
+int idw_warp_deriv_fwd(void *ctx, const double *dxs, int64_t cdof, double *dxv, int64_t ndof, int where);
+
 /* Denominator estimate denominator0 (nvol), in common order.
  * (initializeWarping.F90:241-247) */
 int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where);

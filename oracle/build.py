@@ -31,5 +31,20 @@ def build_oracle(force=False, verbose=False):
     return LIB
 
 
+def build_oracle_contracted():
+    """The same source with FMA contraction (x86-64 with FMA only).  Not a
+    second oracle: comparing the two measures how sensitive a case is to the
+    rounding order of the reference formulas."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    out = os.path.join(OUT_DIR, "liboracle_fma.so")
+    if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
+        return out
+    flags = ["-ffp-contract=fast"] + (["-mfma"] if os.uname().machine == "x86_64" else [])
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp"] + flags + [SRC, "-o", out + ".tmp"],
+                   check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True, verbose=True))

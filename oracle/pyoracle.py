@@ -26,10 +26,18 @@ def _i(a):
     return a.ctypes.data_as(_IP)
 
 
-def lib():
+def use_library(path=None):
+    """Load the oracle from another build of the same source (None: the default
+    build).  Used to measure how sensitive a case is to rounding order."""
+    global _lib
+    _lib = None
+    return lib(path)
+
+
+def lib(path=None):
     global _lib
     if _lib is None:
-        path = build_oracle()
+        path = path or build_oracle()
         L = C.CDLL(path)
         L.orc_new.restype = C.c_void_p
         L.orc_new.argtypes = [_DP]

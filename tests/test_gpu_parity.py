@@ -253,3 +253,56 @@ def test_mixed_deriv_batch_matches_fp64(mode, wing, built_lib):
         out.append(g.warpDerivBatch(seeds))
     scale = np.abs(out[0]).max()
     assert np.abs(out[1] - out[0]).max() <= 1e-6 * scale, np.abs(out[1] - out[0]).max() / scale
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_warp_deriv_fwd_fp64_matches_oracle(case, mode, sphere, wing, built_lib, oracle_lib):
+    # warpDerivFwd against the oracle's complex-step tangent (exact to rounding)
+    m = sphere if case == "sphere" else wing
+    om = build_oracle(m, {"evalMode": mode})
+    g = build_gpu(m, {"evalMode": mode}, precision="fp64")
+    om.set_surface_coordinates(m["xs"])
+    g.setSurfaceCoordinates(m["xs"])
+    om.warp()
+    rng = np.random.default_rng(11)
+    dxs = rng.normal(size=m["pts"].shape)
+    do = om.warp_deriv_fwd(dxs)
+    dg = g.warpDerivFwd(dxs, solverVec=False).reshape(-1, 3)
+    assert np.abs(dg - do).max() <= 1e-10 * np.abs(do).max()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-6)])
+def test_warp_deriv_dot_product(precision, tol, wing, built_lib):
+    # <dXv, J dXs> = <J^T dXv, dXs> between warpDerivFwd and warpDeriv
+    g = build_gpu(wing, precision=precision)
+    g.setSurfaceCoordinates(wing["xs"])
+    g.warpMesh()
+    rng = np.random.default_rng(12)
+    dxs = rng.normal(size=wing["pts"].shape)
+    dxv = rng.normal(size=3 * len(wing["xv0"]))
+    fwd = g.warpDerivFwd(dxs, solverVec=False)
+    g.warpDeriv(dxv, solverVec=False)
+    rev = g.getdXs()
+    a, b = float(np.dot(dxv, fwd)), float(np.sum(rev * dxs))
+    # relative to the sums of |terms| (the products cancel to ~1% of them)
+    scale = max(float(np.sum(np.abs(dxv * fwd))), float(np.sum(np.abs(rev * dxs))))
+    assert abs(a - b) <= tol * scale, (a, b, scale)
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+def test_warp_deriv_fwd_mixed_matches_fp64(mode, sphere, built_lib):
+    g64 = build_gpu(sphere, {"evalMode": mode}, precision="fp64")
+    g32 = build_gpu(sphere, {"evalMode": mode}, precision="mixed")
+    rng = np.random.default_rng(13)
+    dxs = rng.normal(size=sphere["pts"].shape)
+    out = []
+    for g in (g64, g32):
+        g.setSurfaceCoordinates(sphere["xs"])
+        out.append(g.warpDerivFwd(dxs, solverVec=False))
+    assert np.abs(out[1] - out[0]).max() <= 1e-6 * np.abs(out[0]).max()
+    # the mixed tangent walk leaves the mesh state ready for the next warp
+    g32.warpMesh()
+    g64.warpMesh()
+    err = np.abs(g32.getWarpGrid() - g64.getWarpGrid()).max() / g64.getStats()["Ldef0"]
+    assert err < TOL_MIXED
