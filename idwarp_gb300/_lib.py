@@ -16,6 +16,13 @@ IDW_EVAL_EXACT = 0
 IDW_EVAL_FAST = 1
 IDW_PREC_FP64 = 0
 IDW_PREC_MIXED = 1
+IDW_OK = 0
+IDW_ERR_ARG = -1
+IDW_ERR_STATE = -2
+IDW_ERR_CUDA = -3
+IDW_ERR_NONFINITE = -4
+IDW_ERR_LIMIT = -5
+IDW_ERR_NOMEM = -6
 
 _ERRNAMES = {
     -1: "IDW_ERR_ARG", -2: "IDW_ERR_STATE", -3: "IDW_ERR_CUDA", -4: "IDW_ERR_NONFINITE",
@@ -83,6 +90,7 @@ _SIGS = {
     "idw_get_dxs": [_VP, _VP, C.c_int64, C.c_int],
     "idw_warp_deriv_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_warp_deriv_fwd": [_VP, _VP, C.c_int64, _VP, C.c_int64, C.c_int],
+    "idw_warp_deriv_noalloc": [_VP, _VP, C.c_int64, _VP, C.c_int64],
     "idw_get_denominator0": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_denominator": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_stats": [_VP, C.POINTER(idw_stats)],

@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1182,6 +1183,107 @@ int idw_get_nodal_properties(void *ctx, double *mi, double *bi) {
         if (bi) std::memcpy(bi + 3 * i, &mb[12 * i + 9], 3 * sizeof(double));
     }
     return IDW_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// warpDeriv without any allocation, for callers that cannot allocate device
+// memory during the call.  Scratch lives in one file-scope device array whose
+// address is looked up once per device; calls that overlap in time (two
+// contexts, or two streams, at once) share it and race.
+namespace {
+
+constexpr size_t kNoAllocScratchDoubles = size_t(6) << 20;  // 48 MiB
+static __device__ __align__(256) double g_noallocScratch[kNoAllocScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noallocMu;
+double *g_noallocPtr[kMaxDevices] = {};
+
+int noalloc_scratch(Ctx *c, double **out) {
+    if (c->device < 0 || c->device >= kMaxDevices) return fail(c, IDW_ERR_LIMIT, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noallocMu);
+    if (!g_noallocPtr[c->device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess) return fail(c, IDW_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_noallocPtr[c->device] = static_cast<double *>(p);
+    }
+    *out = g_noallocPtr[c->device];
+    return IDW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *dxs, int64_t cdof) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDeriv");
+    if (!dxv || !dxs) return fail(c, IDW_ERR_ARG, "null dXv or dXs");
+    if (ndof != 3 * c->nVol)
+        return fail(c, IDW_ERR_ARG, "dXv has %lld entries, expected %lld", (long long)ndof, (long long)(3 * c->nVol));
+    if (cdof != 3 * int64_t(c->nPts))
+        return fail(c, IDW_ERR_ARG, "dXs has %lld entries, expected %lld", (long long)cdof,
+                    (long long)(3 * int64_t(c->nPts)));
+    const int n = c->nUnique, nn = c->nNodes;
+    const int mixed = c->opt.precision == IDW_PREC_MIXED;
+    const size_t need = 12 * size_t(n) + 12 * size_t(nn) + (mixed ? 12 * size_t(n) : 0);
+    if (need > kNoAllocScratchDoubles)
+        return fail(c, IDW_ERR_LIMIT,
+                    "warpDeriv without allocation needs %zu scratch doubles for %d surface nodes and %d tree nodes; "
+                    "the static scratch holds %zu",
+                    need, n, nn, kNoAllocScratchDoubles);
+    CK(cudaSetDevice(c->device));
+    double *scratch = nullptr;
+    int rc = noalloc_scratch(c, &scratch);
+    if (rc) return rc;
+    double *ptAdj = scratch, *nodeAdj = scratch + 12 * size_t(n), *ptRel = nodeAdj + 12 * size_t(nn);
+    rc = refresh_nodal(c);
+    if (rc) return rc;
+    EvalConsts k;
+    k.law = make_law(c);
+    k.errTol = c->opt.errTol;
+    k.sym = c->sym;
+    k.slotStats = 0;
+    k.precGate = 0.0;
+    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
+    // the accumulators start at zero
+    CK(cudaMemsetAsync(ptAdj, 0, sizeof(double) * 12 * size_t(n), c->stream));
+    CK(cudaMemsetAsync(nodeAdj, 0, sizeof(double) * 12 * size_t(nn), c->stream));
+    CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+    if (mixed) {
+        TreeDevF tf;
+        tf.nodes = c->nodeRec.p;
+        PointsDevF pf;
+        pf.da = c->ptDA.p;
+        pf.dl = c->ptDL.p;
+        pf.dm = c->ptDM.p;
+        pf.dml = c->ptDMl.p;
+        WalkRecF rec;
+        rec.hi = c->recHi.p;
+        rec.lo = c->recLo.p;
+        launch_adjoint_mixed(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxv, 1, ndof, c->den.p, ptAdj, nodeAdj,
+                             ptRel, c->ptXA.p, n, c->counters.p, c->stream);
+    } else {
+        PointsDev p;
+        p.xa = c->ptXA.p;
+        p.mb = c->ptMB.p;
+        launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxv, c->den.p, 1, ndof, ptAdj, nodeAdj,
+                                 int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
+        launch_set_data_b(tree_dev(c), nodeAdj, ptAdj, n, c->stream);
+    }
+    rc = check_launch(c, "adjoint walk");
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->xub.p, 0, sizeof(double) * 3 * size_t(n), c->stream));
+    launch_nodal_b(surf_dev(c), c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations,
+                   mixed ? ptRel : ptAdj, mixed, c->xub.p, c->stream);
+    CK(cudaMemsetAsync(dxs, 0, sizeof(double) * size_t(cdof), c->stream));
+    launch_scatter_dxs(n, c->xuInd.p, c->xub.p, dxs, c->stream);
+    return check_launch(c, "reverse nodal properties");
 }
 
 }  // extern "C"

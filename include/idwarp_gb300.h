@@ -186,6 +186,21 @@ int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *d
  * is divided by that warp's denominator. */
 int idw_warp_deriv_fwd(void *ctx, const double *dxs, int64_t cdof, double *dxv, int64_t ndof, int where);
 
+/* idw_warp_deriv for one seed without allocating device memory in the call,
+ * for callers that cannot allocate while they run (memory reserved up front,
+ * allocation-free solver loops).  No reference counterpart.  dxv (nvol,3)
+ * and dxs (npts,3, receives the result) are device pointers; the work is
+ * ordered on the context's stream and not synchronised.  Scratch is one
+ * static 48 MiB device array shared by every context of the process:
+ * 12 doubles per unique surface node and per tree node, plus 12 per surface
+ * node in mixed precision, must fit in 6*2^20 doubles (with bucketSize 8
+ * about 210k unique surface nodes in mixed precision, 360k in FP64), else
+ * IDW_ERR_LIMIT.  Calls that overlap in time
+ * (several contexts or streams at once) race on that scratch.  The first
+ * call on a device looks the scratch up (cudaGetSymbolAddress): make it
+ * before any stream capture. */
+int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *dxs, int64_t cdof);
+
 /* Denominator estimate denominator0 (nvol), in common order.
  * (initializeWarping.F90:241-247) */
 int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where);
