@@ -101,6 +101,7 @@ class USMesh(BaseSolver):
             "bucketSize": [int, 8],
             "precision": [str, ["mixed", "fp64"]],
             "mixedGate": [float, 2e-3],
+            "diagnostics": [int, 0],
         }
 
     # ------------------------------------------------------------------
@@ -474,6 +475,7 @@ class USMesh(BaseSolver):
         o.evalMode = _lib.IDW_EVAL_FAST if self.getOption("evalMode") == "fast" else _lib.IDW_EVAL_EXACT
         o.precision = _lib.IDW_PREC_MIXED if self.getOption("precision") == "mixed" else _lib.IDW_PREC_FP64
         o.mixedGate = self.getOption("mixedGate")
+        o.diagnostics = self.getOption("diagnostics")
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

@@ -73,36 +73,23 @@ __device__ __forceinline__ int4 ldgi4(const int4 *p) { return __ldg(p); }
 // the radii 2,3,4,5,7.5,10,20,40,...,640: unit steps below 5, then 7.5 and 10,
 // then doublings from 20.  Returns err, sets bnd.
 __device__ __forceinline__ float get_error32(const float *e, float dOvrR, float &bnd) {
-    int i;
-    float r0, r1;
-    if (dOvrR < 5.0f) {
-        i = int(dOvrR) - 2;  // 0..2
-        r0 = float(i + 2);
-        r1 = r0 + 1.0f;
-    } else if (dOvrR < 10.0f) {
-        i = dOvrR < 7.5f ? 3 : 4;
-        r0 = i == 3 ? 5.0f : 7.5f;
-        r1 = i == 3 ? 7.5f : 10.0f;
-    } else if (dOvrR < 20.0f) {
-        i = 5;
-        r0 = 10.0f;
-        r1 = 20.0f;
-    } else if (dOvrR < 640.0f) {
-        // 20 * 2^m <= dOvrR < 20 * 2^(m+1), m = 0..4
-        const int m = ((__float_as_int(dOvrR * 0.05f) >> 23) & 0xff) - 127;
-        i = 6 + m;
-        r0 = 20.0f * float(1 << m);
-        r1 = 2.0f * r0;
-    } else {
-        const float e11 = __ldg(e + kNerr - 1);
-        bnd = 2e-6f * fabsf(e11);
-        return e11;
-    }
-    const float orst = 1.0f / (r1 - r0);
+    // Bracket [r0, r1) and 1/(r1 - r0) by selects, so lanes in different
+    // brackets do not diverge; the values equal the reference's bracket and
+    // the correctly rounded reciprocal (1, 0.4, 0.4, 0.1, 0.05 * 2^-m).
+    const float d = dOvrR;
+    const float fl = floorf(d);
+    // 20 * 2^m <= d < 20 * 2^(m+1) for d in [20, 640), m = 0..4
+    const int m = min(4, max(0, ((__float_as_int(d * 0.05f) >> 23) & 0xff) - 127));
+    const float p2 = __int_as_float((127 + m) << 23), ip2 = __int_as_float((127 - m) << 23);
+    const bool a = d < 5.0f, b = d < 7.5f, c = d < 10.0f, t = d < 20.0f, far = d >= 640.0f;
+    int i = a ? int(fl) - 2 : (b ? 3 : (c ? 4 : (t ? 5 : 6 + m)));
+    const float r0 = a ? fl : (b ? 5.0f : (c ? 7.5f : (t ? 10.0f : 20.0f * p2)));
+    const float orst = a ? 1.0f : (c ? 0.4f : (t ? 0.1f : 0.05f * ip2));
+    i = far ? kNerr - 2 : i;
     const float e0 = __ldg(e + i), e1 = __ldg(e + i + 1);
-    const float fact = (dOvrR - r0) * orst;
-    bnd = 2e-6f * (dOvrR * orst * fabsf(e1 - e0) + fabsf(e0) + fabsf(e1));
-    return (1.0f - fact) * e0 + fact * e1;
+    const float fact = (d - r0) * orst;
+    bnd = far ? 2e-6f * fabsf(e1) : 2e-6f * (d * orst * fabsf(e1 - e0) + fabsf(e0) + fabsf(e1));
+    return far ? e1 : (1.0f - fact) * e0 + fact * e1;
 }
 
 // Exact difference a - b as (hi, lo) (Knuth two-sum).

@@ -333,32 +333,30 @@ __global__ void k_nodal(SurfaceDev s, const double *Xu, const dbl4 *xa, const do
 }
 
 // setData: unweighted mean of the 12 node values over each interior node's
-// range; one block per interior node.
+// range (kd_tree.F90:595-617); one warp per node, lanes stride the range.
 __global__ void k_set_data(TreeDev t, const double *ptMB, double *nodeMB) {
-    int q = blockIdx.x;
+    const int q = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (q >= t.nNodes) return;
-    int4 inf = t.info[q];
+    const int4 inf = t.info[q];
     if (inf.w) return;  // leaves carry no aggregate
     double acc[12];
 #pragma unroll
     for (int c = 0; c < 12; ++c) acc[c] = 0.0;
-    for (int i = inf.x + threadIdx.x; i <= inf.y; i += blockDim.x) {
-        const double *p = ptMB + 12 * i;
+    for (int i = inf.x + lane; i <= inf.y; i += 32) {
+        const double2 *p = reinterpret_cast<const double2 *>(ptMB + 12 * i);
 #pragma unroll
-        for (int c = 0; c < 12; ++c) acc[c] += p[c];
+        for (int c = 0; c < 6; ++c) {
+            const double2 v = __ldg(p + c);
+            acc[2 * c] += v.x;
+            acc[2 * c + 1] += v.y;
+        }
     }
-    __shared__ double red[12][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const double cnt = double(inf.y - inf.x + 1);
 #pragma unroll
     for (int c = 0; c < 12; ++c) {
-        double v = warp_sum(acc[c]);
-        if (lane == 0) red[c][wid] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 12) {
-        double v = 0.0;
-        for (int w = 0; w < int(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
-        nodeMB[12 * q + threadIdx.x] = v / double(inf.y - inf.x + 1);
+        const double v = warp_sum(acc[c]);
+        if (lane == c) nodeMB[12 * q + c] = v / cnt;
     }
 }
 
@@ -615,7 +613,7 @@ void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const d
         k_nodal<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, Ai, isCorner, useRotations, ptMB);
 }
 void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, cudaStream_t st) {
-    if (t.nNodes > 0) k_set_data<<<t.nNodes, 128, 0, st>>>(t, ptMB, nodeMB);
+    if (t.nNodes > 0) k_set_data<<<blocks(int64_t(t.nNodes) * 32, 128), 128, 0, st>>>(t, ptMB, nodeMB);
 }
 void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st) {
     if (nPts > 0) k_set_data_b<<<blocks(nPts, 128), 128, 0, st>>>(t, nodeAdj, ptAdj, nPts);
