@@ -72,6 +72,11 @@ struct Ctx {
     DevBuf<float4> ptDA, ptDL;
     DevBuf<float4> recHi, recLo, acc;  // per-volume-node walk records and accumulators
     DevBuf<float> gden;                // per node: scaled denominator of a mixed walk (precision gate)
+    // per-surface state of the batched mixed walk (grown on demand)
+    int batchCap = 0;
+    DevBuf<double> bXs, bXu, bPtMB, bNodeMB;
+    DevBuf<float> bPtDM, bPtDMl, bNodeDC, bNodeDCl, bNodeDn, bRef;
+    DevBuf<float4> bAcc;
     bool gdenValid = false;
     double gdenLdefFact = 0.0, gdenAlpha = 0.0;
     int gdenMode = -1;
@@ -721,6 +726,82 @@ int idw_warp_mesh(void *ctx) {
     return IDW_OK;
 }
 
+}  // extern "C"
+
+// Up to kBatchWalk surfaces share one mixed walk (idw_batch.cu): per surface
+// the nodal properties, cluster means and FP32 motion arrays, then one walk
+// and a finalisation per surface.  coords/out are device pointers.
+static constexpr int kBatchWalk = 4;
+
+static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double *outDev) {
+    const int n = c->nUnique, nn = c->nNodes;
+    const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
+    if (c->batchCap < nb) {
+        const size_t B = kBatchWalk;
+        CKA(c->bXu.alloc(B * 3 * n));
+        CKA(c->bPtMB.alloc(B * 12 * n));
+        CKA(c->bNodeMB.alloc(B * 12 * size_t(nn)));
+        CKA(c->bPtDM.alloc(B * 12 * n));
+        CKA(c->bPtDMl.alloc(B * 12 * n));
+        CKA(c->bNodeDC.alloc(B * 12 * size_t(nn)));
+        CKA(c->bNodeDCl.alloc(B * 12 * size_t(nn)));
+        CKA(c->bNodeDn.alloc(B * size_t(nn)));
+        CKA(c->bRef.alloc(B * 24));
+        CKA(c->bAcc.alloc(B * 2 * size_t(c->nVol)));
+        c->batchCap = kBatchWalk;
+    }
+    SurfaceDev s = surf_dev(c);
+    for (int b = 0; b < nb; ++b) {
+        double *xu = c->bXu.p + size_t(b) * 3 * n, *mb = c->bPtMB.p + size_t(b) * 12 * n;
+        double *nmb = c->bNodeMB.p + size_t(b) * 12 * nn;
+        launch_gather_xu(n, c->xuInd.p, coordsDev + size_t(b) * sdof, xu, c->stream);
+        launch_nodal(s, xu, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, mb, c->stream);
+        launch_set_data(tree_dev(c), mb, nmb, c->stream);
+        launch_mixed_nodal(n, tree_dev(c), nmb, c->ptXA.p, mb, c->bPtDM.p + size_t(b) * 12 * n,
+                           c->bPtDMl.p + size_t(b) * 12 * n, c->stream);
+        launch_mixed_nodes(tree_dev(c), nmb, mb, c->bNodeDC.p + size_t(b) * 12 * nn, c->bNodeDCl.p + size_t(b) * 12 * nn,
+                           c->bNodeDn.p + size_t(b) * nn, c->bRef.p + 24 * b, c->stream);
+    }
+    int rc = check_launch(c, "batch nodal properties");
+    if (rc) return rc;
+    EvalConsts k;
+    k.law = make_law(c);
+    k.errTol = c->opt.errTol;
+    k.sym = c->sym;
+    k.slotStats = 0;
+    k.precGate = c->opt.mixedGate * c->Ldef0 * c->opt.LdefFact;
+    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
+    TreeDevF tf;
+    tf.nodes = c->nodeRec.p;
+    PointsDevF pf;
+    pf.da = c->ptDA.p;
+    pf.dl = c->ptDL.p;
+    pf.dm = c->bPtDM.p;
+    pf.dml = c->bPtDMl.p;
+    NodeAggF af;
+    af.dc = c->bNodeDC.p;
+    af.dcl = c->bNodeDCl.p;
+    af.dn = c->bNodeDn.p;
+    af.ref = c->bRef.p;
+    WalkRecF rec;
+    rec.hi = c->recHi.p;
+    rec.lo = c->recLo.p;
+    rc = ensure_gate_den(c, tf, pf, af, rec, k, exact);
+    if (rc) return rc;
+    rec.gden = c->gden.p;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    launch_walk_mixed_batch(nb, tree_dev(c), tf, pf, 12 * int64_t(n), af, 12 * int64_t(nn), int64_t(nn), vol_dev(c),
+                            rec, k, exact, c->bAcc.p, 2 * c->nVol, c->counters.p, c->stream);
+    for (int b = 0; b < nb; ++b)
+        launch_finalize_mixed(vol_dev(c), rec, c->bAcc.p + size_t(b) * 2 * c->nVol, k.law.bExp,
+                              outDev + size_t(b) * vdof, c->stream);
+    CK(cudaEventRecord(c->ev1, c->stream));
+    c->eventsRecorded = true;
+    return check_launch(c, "batch walk");
+}
+
+extern "C" {
+
 int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double *out, int where) {
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
@@ -728,6 +809,35 @@ int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double 
     if (nbatch < 0 || !coords || !out) return fail(c, IDW_ERR_ARG, "bad batch arguments");
     CK(cudaSetDevice(c->device));
     const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
+    if (c->opt.precision == IDW_PREC_MIXED && nbatch > 0) {
+        // surfaces in groups of up to kBatchWalk per walk
+        CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+        DevBuf<double> tin, tout;
+        const int g = std::min<int>(nbatch, kBatchWalk);
+        if (where != IDW_DEVICE) {
+            CKA(tin.alloc(size_t(g) * sdof));
+            CKA(tout.alloc(size_t(g) * vdof));
+        }
+        for (int b0 = 0; b0 < nbatch; b0 += kBatchWalk) {
+            const int nb = std::min<int>(kBatchWalk, nbatch - b0);
+            const double *cin = coords + size_t(b0) * sdof;
+            double *cout = out + size_t(b0) * vdof;
+            if (where != IDW_DEVICE) {
+                if (!all_finite(cin, size_t(nb) * sdof)) return fail(c, IDW_ERR_NONFINITE, "non-finite coordinates");
+                int rc = copy_in(c, tin.p, cin, size_t(nb) * sdof, IDW_HOST);
+                if (rc) return rc;
+                cin = tin.p;
+            }
+            int rc = run_warp_batch_mixed(c, cin, nb, where != IDW_DEVICE ? tout.p : cout);
+            if (rc) return rc;
+            if (where != IDW_DEVICE) {
+                rc = copy_out(c, out + size_t(b0) * vdof, tout.p, size_t(nb) * vdof, IDW_HOST);
+                if (rc) return rc;
+            }
+        }
+        CK(cudaStreamSynchronize(c->stream));
+        return IDW_OK;
+    }
     // keep the context's own surface: stage it and restore afterwards
     DevBuf<double> keep, tmpOut;
     CKA(keep.alloc(sdof));

@@ -152,6 +152,15 @@ int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeD
                              double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
                              unsigned long long *counters, cudaStream_t st);
 MixedParams make_mixed_params(const EvalConsts &k);
+// nb (1..4) surfaces in one mixed walk (idw_batch.cu): per-surface point and
+// cluster arrays at strides ptStrideB / nodeStrideB / dnStrideB (floats), the
+// reference motions at af.ref + 24 b, accumulators at acc + accStrideB * b.
+void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, int64_t ptStrideB,
+                             const NodeAggF &af, int64_t nodeStrideB, int64_t dnStrideB, const VolumeDev &v,
+                             const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc, int64_t accStrideB,
+                             unsigned long long *counters, cudaStream_t st);
+void launch_finalize_mixed(const VolumeDev &v, const WalkRecF &rec, const float4 *acc, double bExp, double *xv,
+                           cudaStream_t st);
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,

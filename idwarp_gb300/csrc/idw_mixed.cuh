@@ -176,21 +176,21 @@ __device__ __forceinline__ void comp_add_df(float &s, float &c, float h, float l
 // would show in Xv: x (hi + lo) is the volume point relative to the term's
 // reference point (a surface point, or a cluster centroid), eps the distance
 // softening (1e-15 for surface points, 0 for clusters), A (hi + lo) the area,
-// and S = D x + c with D (9) and c (3) from the hi/lo arrays dh, dl.  Adds
-// w S and w to the compensated pairs.  Specialised to the default exponents
-// (3, 5); others go through the generic double-float routines.
+// and S = D x + c with D (9) and c (3) from the hi/lo arrays dh, dl.
+// precise_weight returns the renormalised x and the weight w (hi + lo),
+// specialised to the default exponents (3, 5), other exponents through the
+// generic double-float routines; precise_motion adds w S to a compensated
+// pair; precise_term is both, and adds w to the denominator pair.
 template <int KIND>
-__device__ __forceinline__ void precise_term(const dfl xin[3], float eps, float Ah, float Al, const float *dh,
-                                             const float *dl, const Law32<KIND> &law, float Ls, float LsLo, float c1,
-                                             float abH, float abL, float *sn, float *cn, float &sd, float &cd) {
+__device__ __forceinline__ void precise_weight(const dfl xin[3], float eps, float Ah, float Al, const Law32<KIND> &law,
+                                               float Ls, float LsLo, float c1, float abH, float abL, dfl x[3],
+                                               float &wh, float &wl) {
     // x arrives as an exact difference plus a correction that can be as
     // large as the difference itself (a volume node on a surface node:
     // hi = -lo); renormalise so that |lo| <= ulp(hi) / 2, which the
     // products below assume (they drop lo * lo)
-    dfl x[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) two_sum(xin[k].h, xin[k].l, x[k].h, x[k].l);
-    float wh, wl;
     if (KIND == 0) {
         // d^2 = |x|^2 + eps
         const float p0 = x[0].h * x[0].h, p1 = x[1].h * x[1].h, p2 = x[2].h * x[2].h;
@@ -244,6 +244,10 @@ __device__ __forceinline__ void precise_term(const dfl xin[3], float eps, float 
         wh = w.h;
         wl = w.l;
     }
+}
+
+__device__ __forceinline__ void precise_motion(const dfl x[3], float wh, float wl, const float *dh, const float *dl,
+                                               float *sn, float *cn) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         // S_a = c_a + sum_k D_ak x_k, each product split exactly, sums by two-sum
@@ -262,6 +266,17 @@ __device__ __forceinline__ void precise_term(const dfl xin[3], float eps, float 
         const float ql = fmaf(wl, Sh, fmaf(wh, Sl, fmaf(wh, Sh, -qh)));
         comp_add_df(sn[a], cn[a], qh, ql);
     }
+}
+
+
+template <int KIND>
+__device__ __forceinline__ void precise_term(const dfl xin[3], float eps, float Ah, float Al, const float *dh,
+                                             const float *dl, const Law32<KIND> &law, float Ls, float LsLo, float c1,
+                                             float abH, float abL, float *sn, float *cn, float &sd, float &cd) {
+    dfl x[3];
+    float wh, wl;
+    precise_weight<KIND>(xin, eps, Ah, Al, law, Ls, LsLo, c1, abH, abL, x, wh, wl);
+    precise_motion(x, wh, wl, dh, dl, sn, cn);
     comp_add_df(sd, cd, wh, wl);
 }
 

@@ -146,9 +146,12 @@ int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int whe
  * src/warp/warpMesh.F90:1-82) */
 int idw_warp_mesh(void *ctx);
 
-/* Warp nbatch surfaces in one call: coords holds nbatch stacked (npts,3)
- * surfaces, out receives nbatch stacked (nvol,3) grids.  The context's stored
- * surface/grid are left unchanged.  No reference counterpart. */
+/* Warp nbatch surfaces (perturbations of the same surface definition) in one
+ * call: coords holds nbatch stacked (npts,3) surfaces, out receives nbatch
+ * stacked (nvol,3) grids.  In mixed precision up to four surfaces share one
+ * tree walk (decisions and weights computed once); in FP64 the surfaces are
+ * warped one after the other.  The context's stored surface/grid are left
+ * unchanged.  No reference counterpart. */
 int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double *out, int where);
 
 /* Current volume grid in warp order (== common order on one GPU).

@@ -306,3 +306,34 @@ def test_warp_deriv_fwd_mixed_matches_fp64(mode, sphere, built_lib):
     g64.warpMesh()
     err = np.abs(g32.getWarpGrid() - g64.getWarpGrid()).max() / g64.getStats()["Ldef0"]
     assert err < TOL_MIXED
+
+
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+@pytest.mark.parametrize("case", ["sphere", "wing"])
+def test_mixed_batch_walk_matches_fp64(case, mode, sphere, wing, built_lib):
+    # five surfaces: one shared walk of four, then one of one
+    from idwarp_gb300 import synthetic as S
+
+    m = sphere if case == "sphere" else wing
+    pert = S.sphere_perturbation if case == "sphere" else S.wing_perturbation
+    surfaces = np.stack([pert(m["pts"], seed=200 + i) for i in range(5)])
+    g64 = build_gpu(m, {"evalMode": mode}, precision="fp64")
+    g32 = build_gpu(m, {"evalMode": mode}, precision="mixed")
+    out = g32.warpMeshBatch(surfaces)
+    st = g32.getStats()
+    L = g64.getStats()["Ldef0"]
+    for b in range(5):
+        g64.setSurfaceCoordinates(surfaces[b])
+        g64.warpMesh()
+        err = np.abs(out[b] - g64.getWarpGrid().reshape(-1, 3)).max() / L
+        assert err < TOL_MIXED, (b, err)
+    # the stored surface and grid of the mesh are left alone
+    g32.setSurfaceCoordinates(m["xs"])
+    g32.warpMesh()
+    g64.setSurfaceCoordinates(m["xs"])
+    g64.warpMesh()
+    assert np.abs(g32.getWarpGrid() - g64.getWarpGrid()).max() / L < TOL_MIXED
+    # decisions are those of one walk per group
+    s64 = g64.getStats()
+    assert st["leafPairs"] == 2 * s64["leafPairs"]
+    assert st["approx"] == 2 * s64["approx"]
