@@ -124,6 +124,14 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def _measured_peak(key):
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f).get(key)
+    except Exception:
+        return None
+
+
 def fp32_peak_tflops():
     """Measured FFMA issue peak of this GPU (TFLOP/s) from a dependent-chain-free FMA probe."""
     import torch
@@ -181,6 +189,146 @@ def run_cpu_baseline(m, budget_s=15.0, threads=None, seed=0):
                 n, nvol, ERR_TOL, dt)}
 
 
+def _timed(fn, reps, stream):
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_suite():
+    """The measurement table: S1 sphere, W wing, P wing errTol sweep; one JSON line per row.
+
+    Per row: GPU mixed and FP64 times (CUDA events on the library's stream,
+    device-resident surface), the precision error of the mixed form against
+    FP64 on the same tree and decisions, the algorithmic error of fast against
+    exact mode, and the oracle on the host cores (all threads, and one) on a
+    seeded sample of volume nodes."""
+    import torch
+
+    from idwarp_gb300 import _lib
+    from idwarp_gb300 import synthetic as S
+    from oracle.pyoracle import OracleMesh, max_threads, set_threads
+
+    stream = torch.cuda.current_stream()
+    nthreads = max_threads()
+
+    def gpu_mesh(m, prec, mode, errTol):
+        o = mesh_options(m, prec, mode)
+        o["errTol"] = errTol
+        with contextlib.redirect_stdout(io.StringIO()):
+            g = USMesh_(o)
+            g.createCommonGrid(m["xv0"])
+            g.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
+        g.lib.idw_set_stream(g.ctx, C.c_void_p(stream.cuda_stream))
+        return g
+
+    def cpu_rate(m, mode, errTol, threads, budget):
+        set_threads(threads)
+        rng = np.random.default_rng(7)
+        nvol = len(m["xv0"])
+        n = min(nvol, 2000 if mode == "exact" else 20000)
+        for attempt in range(2):
+            idx = np.sort(rng.choice(nvol, n, replace=False))
+            o = dict(mesh_options(m, "fp64", mode))
+            o["errTol"] = errTol
+            om = OracleMesh({k: o[k] for k in ("aExp", "bExp", "LdefFact", "alpha", "errTol", "evalMode", "bucketSize")})
+            om.set_volume(m["xv0"][idx])
+            if m.get("symmetryPlanes"):
+                planes = m["symmetryPlanes"]
+                om.set_symmetry(np.array([p[0] for p in planes]), np.array([p[1] for p in planes]))
+            om.set_surface_definition(m["pts"], m["conn"], m["faceSizes"])
+            om.set_surface_coordinates(m["xs"])
+            t0 = time.perf_counter()
+            om.warp()
+            dt = time.perf_counter() - t0
+            if attempt == 0 and dt < budget and n < nvol:
+                n = int(min(nvol, n * budget / max(dt, 1e-3)))
+                continue
+            break
+        set_threads(nthreads)
+        return n / dt, n
+
+    from idwarp_gb300 import USMesh as USMesh_
+
+    sph = S.sphere_ogrid(n=18, layers=48)
+    sph["xs"] = S.sphere_perturbation(sph["pts"], seed=0)
+    rows = [("S1_sphere_95k", sph, [1e-4]), ("W_wing_2M", make_workload("W"), [1e-4]),
+            ("P_wing_8M", make_workload("P"), [1e-3, 1e-4, 1e-5])]
+    for name, m, tols in rows:
+        nvol = len(m["xv0"])
+        for errTol in tols:
+            res = {"row": name, "volume_nodes": nvol, "surface_points": len(m["pts"]), "errTol": errTol}
+            xs_dev = torch.tensor(m["xs"], dtype=torch.float64, device="cuda")
+            grids = {}
+            modes = ["fast", "exact"] if name != "P_wing_8M" else ["fast"]
+            for mode in modes:
+                for prec in ("mixed", "fp64"):
+                    if prec == "fp64" and mode == "exact" and nvol > 3e5:
+                        continue  # minutes of FP64 pairs; the mixed exact result stands in
+                    g = gpu_mesh(m, prec, mode, errTol)
+
+                    def step(g=g):
+                        g.lib.idw_set_surface_coordinates(g.ctx, C.c_void_p(xs_dev.data_ptr()), xs_dev.numel(),
+                                                          _lib.IDW_DEVICE)
+                        g.lib.idw_warp_mesh(g.ctx)
+
+                    ms = _timed(step, 2 if (prec == "fp64" or mode == "exact") else 5, stream)
+                    grids[(mode, prec)] = g.getWarpGrid().reshape(-1, 3)
+                    st = g.getStats()
+                    res["%s_%s_ms" % (mode, prec)] = ms
+                    res["%s_%s_nodes_per_s" % (mode, prec)] = nvol / (ms * 1e-3)
+                    res["%s_PI" % mode] = st["leafPairs"] + st["approx"]
+                    if mode == "fast" and errTol == 1e-4 and name != "P_wing_8M":
+                        rng = np.random.default_rng(1)
+                        seed = torch.tensor(rng.normal(size=3 * nvol), device="cuda")
+                        dxs = torch.empty(3 * len(m["pts"]), dtype=torch.float64, device="cuda")
+
+                        def deriv(g=g):
+                            g.lib.idw_warp_deriv_batch(g.ctx, C.c_void_p(seed.data_ptr()), 1, C.c_void_p(dxs.data_ptr()),
+                                                       _lib.IDW_DEVICE)
+
+                        res["warpDeriv1_%s_ms" % prec] = _timed(deriv, 2, stream)
+                    del g
+                Ldef = None
+            # precision error (same tree, same decisions) and algorithmic error
+            ref = grids[("fast", "fp64")]
+            gL = gpu_mesh(m, "fp64", "fast", errTol)
+            Ldef = gL.getStats()["Ldef0"]
+            del gL
+            e = np.abs(grids[("fast", "mixed")] - ref).max(axis=1) / Ldef
+            res["fast_mixed_vs_fp64_max_over_Ldef"] = float(e.max())
+            res["fast_mixed_vs_fp64_rms_over_Ldef"] = float(np.sqrt(np.mean(e ** 2)))
+            if ("exact", "fp64") in grids:
+                e = np.abs(grids[("exact", "mixed")] - grids[("exact", "fp64")]).max(axis=1) / Ldef
+                res["exact_mixed_vs_fp64_max_over_Ldef"] = float(e.max())
+                exact_ref = grids[("exact", "fp64")]
+            elif ("exact", "mixed") in grids:
+                exact_ref = grids[("exact", "mixed")]
+            else:
+                exact_ref = None
+            if exact_ref is not None:
+                res["fast_fp64_vs_exact_max_over_Ldef"] = float((np.abs(ref - exact_ref).max(axis=1) / Ldef).max())
+            # the oracle on the host cores
+            budget = 6.0
+            r_all, n_all = cpu_rate(m, "fast", errTol, nthreads, budget)
+            r_one, n_one = cpu_rate(m, "fast", errTol, 1, budget / 2)
+            res["cpu_fast_nodes_per_s_all_cores"] = r_all
+            res["cpu_fast_nodes_per_s_1_core"] = r_one
+            res["cpu_cores"] = nthreads
+            res["cpu_sample_nodes"] = [n_all, n_one]
+            print(json.dumps(res), flush=True)
+            del grids
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -190,7 +338,13 @@ def main():
     ap.add_argument("--config", default="P", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--suite", action="store_true", help="measurement table rows (S1, W, P errTol sweep)")
     args = ap.parse_args()
+    if args.suite:
+        import torch
+
+        torch.cuda.set_device(_env_int("LOCAL_RANK", 0))
+        return run_suite()
 
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -316,10 +470,18 @@ def main():
     flops = 42.0 * (st["leafPairs"] + st["approx"])
     peak = fp32_peak_tflops() if not args.no_extras else None
     achieved = flops / (kernel_ms * 1e-3) / 1e12 if kernel_ms > 0 else None
+    # DRAM traffic of the walk: ncu dram__bytes_read.sum + dram__bytes_write.sum of
+    # k_walk_mixed on the 2M-node wing (148.4 + 42.0 MB for 2,025,050 volume
+    # nodes, profiles/k_walk_mixed_wing2M_full.md), scaled by volume nodes: the
+    # traffic is the per-node records and accumulators, the tree stays in L2
+    traffic = 94.0 * nvol
     out["roofline"] = {"bound": "fp32", "kernel": "k_walk_mixed", "achieved": achieved, "unit": "TFLOP/s",
                        "peak": peak, "peak_source": "measured FFMA probe (idw_probe_ffma) in this run",
                        "frac": (achieved / peak) if (achieved and peak) else None,
-                       "flops_per_launch": flops, "kernel_ms": kernel_ms, "traffic": None}
+                       "flops_per_launch": flops, "kernel_ms": kernel_ms, "traffic": traffic,
+                       "traffic_note": "bytes per launch, ncu on the 2M-node wing scaled by volume nodes",
+                       "hbm": {"achieved_GBs": traffic / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else None,
+                               "peak_GBs": _measured_peak("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"}}
 
     if not args.no_extras:
         # FP64 plain GPU form on the same workload, and the precision of the mixed form against it
@@ -381,6 +543,35 @@ def main():
                             "speedup_mixed_over_fp64": msd64 / msd,
                             "max_rel_diff_vs_fp64": float((dxs - dxs64).abs().max().item() / dref)}
         del sd, dxs, dxs64
+        # 8 independent surface perturbations (seeds 200-207) through the batched
+        # walk (four surfaces share one tree walk) against one warpMesh each
+        from idwarp_gb300 import synthetic as S
+
+        surf = np.stack([S.wing_perturbation(m["pts"], seed=200 + i) for i in range(8)])
+        sb = torch.tensor(surf, dtype=torch.float64, device="cuda")
+        ob = torch.empty((8, nvol, 3), dtype=torch.float64, device="cuda")
+
+        def batch():
+            rc = L.idw_warp_mesh_batch(mesh.ctx, C.c_void_p(sb.data_ptr()), 8, C.c_void_p(ob.data_ptr()),
+                                       _lib.IDW_DEVICE)
+            if rc != 0:
+                _lib.check(L, mesh.ctx, rc, "warpMeshBatch")
+
+        batch()  # warm-up
+        barrier()
+        e0.record(stream)
+        for _ in range(2):
+            batch()
+        e1.record(stream)
+        barrier()
+        msb = e0.elapsed_time(e1) / 2
+        m64.setSurfaceCoordinates(surf[7])
+        m64.warpMesh()
+        errb = np.abs(ob[7].cpu().numpy() - m64.getWarpGrid().reshape(-1, 3)).max() / Ldef
+        out["warpMeshBatch"] = {"surfaces": 8, "value": 8 * nvol / (msb * 1e-3), "unit": "volume nodes/s",
+                                "ms": msb, "ms_per_surface": msb / 8, "speedup_per_surface_over_single": ms_step * 8 / msb,
+                                "max_err_over_Ldef_vs_fp64": float(errb)}
+        del sb, ob
 
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = run_cpu_baseline(m)

@@ -65,7 +65,9 @@ struct Ctx {
     double Ldef0 = 0.0;
     DevBuf<int4> info;
     DevBuf<dbl4> geom;
-    DevBuf<double> nodeErr, nodeAi, nodeMB;
+    DevBuf<double> nodeErr, nodeAi, nodeMB, nodeSum;
+    DevBuf<int> parent;
+    DevBuf<unsigned> nodeFlags;
     bool haveTree = false, haveWarp = false, nodalValid = false;
     // FP32 companion arrays of the mixed-precision walk
     DevBuf<NodeRecF> nodeRec;
@@ -171,7 +173,15 @@ TreeDev tree_dev(Ctx *c) {
     t.geom = c->geom.p;
     t.err = c->nodeErr.p;
     t.ai = c->nodeAi.p;
+    t.parent = c->parent.p;
     return t;
+}
+
+SetDataScratch setdata_scratch(Ctx *c) {
+    SetDataScratch sc;
+    sc.sum = c->nodeSum.p;
+    sc.flags = c->nodeFlags.p;
+    return sc;
 }
 
 SurfaceDev surf_dev(Ctx *c) {
@@ -211,7 +221,7 @@ int refresh_nodal(Ctx *c) {
     launch_gather_xu(c->nUnique, c->xuInd.p, c->xs.p, c->xu.p, c->stream);
     launch_nodal(s, c->xu.p, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, c->ptMB.p,
                  c->stream);
-    launch_set_data(tree_dev(c), c->ptMB.p, c->nodeMB.p, c->stream);
+    launch_set_data(tree_dev(c), c->ptMB.p, c->nodeMB.p, setdata_scratch(c), c->stream);
     if (c->opt.precision == IDW_PREC_MIXED) {
         launch_mixed_nodal(c->nUnique, tree_dev(c), c->nodeMB.p, c->ptXA.p, c->ptMB.p, c->ptDM.p, c->ptDMl.p,
                            c->stream);
@@ -480,6 +490,9 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->nodeErr.alloc(kNerr * size_t(nn)));
     CKA(c->nodeAi.alloc(nn));
     CKA(c->nodeMB.alloc(12 * size_t(nn)));
+    CKA(c->nodeSum.alloc(12 * size_t(nn)));
+    CKA(c->nodeFlags.alloc(size_t(nn)));
+    CKA(c->parent.alloc(size_t(nn)));
     CKA(c->nodeAdj.alloc(12 * size_t(nn)));
     CKA(c->nodeRec.alloc(nn));
     CKA(c->nodeDC.alloc(12 * size_t(nn)));
@@ -507,6 +520,7 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     }
     CK(cudaMemcpyAsync(c->info.p, info.data(), sizeof(int4) * nn, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->geom.p, geom.data(), sizeof(dbl4) * nn, cudaMemcpyHostToDevice, st));
+    launch_tree_parents(tree_dev(c), c->parent.p, st);
     // initial nodal properties: normals0, Ai, corners (kd_tree.F90:1547-1578)
     SurfaceDev s = surf_dev(c);
     launch_gather_xu(n, c->xuInd.p, c->xs.p, c->xu.p, st);
@@ -731,7 +745,7 @@ int idw_warp_mesh(void *ctx) {
 // Up to kBatchWalk surfaces share one mixed walk (idw_batch.cu): per surface
 // the nodal properties, cluster means and FP32 motion arrays, then one walk
 // and a finalisation per surface.  coords/out are device pointers.
-static constexpr int kBatchWalk = 4;
+static constexpr int kBatchWalk = kBatchMax;
 
 static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double *outDev) {
     const int n = c->nUnique, nn = c->nNodes;
@@ -756,7 +770,7 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
         double *nmb = c->bNodeMB.p + size_t(b) * 12 * nn;
         launch_gather_xu(n, c->xuInd.p, coordsDev + size_t(b) * sdof, xu, c->stream);
         launch_nodal(s, xu, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, mb, c->stream);
-        launch_set_data(tree_dev(c), mb, nmb, c->stream);
+        launch_set_data(tree_dev(c), mb, nmb, setdata_scratch(c), c->stream);
         launch_mixed_nodal(n, tree_dev(c), nmb, c->ptXA.p, mb, c->bPtDM.p + size_t(b) * 12 * n,
                            c->bPtDMl.p + size_t(b) * 12 * n, c->stream);
         launch_mixed_nodes(tree_dev(c), nmb, mb, c->bNodeDC.p + size_t(b) * 12 * nn, c->bNodeDCl.p + size_t(b) * 12 * nn,
@@ -1089,7 +1103,7 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
     // (Md + I, bd): the forward walk with S = (Md + I) r + bd - r = Md r + bd
     launch_nodal_d(surf_dev(c), c->xu.p, xud.p, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p,
                    c->opt.useRotations, 1, ptMBd.p, c->stream);
-    launch_set_data(tree_dev(c), ptMBd.p, nodeMBd.p, c->stream);
+    launch_set_data(tree_dev(c), ptMBd.p, nodeMBd.p, setdata_scratch(c), c->stream);
     int rc = check_launch(c, "tangent nodal properties");
     if (rc) return rc;
     EvalConsts k;

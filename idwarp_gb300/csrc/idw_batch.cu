@@ -17,6 +17,11 @@ namespace {
 
 constexpr int kFlush = 4;  // cluster terms per FP32 partial
 
+// Resident blocks per SM the register allocation targets (128 threads each).
+#ifndef IDW_BATCH_MIN_BLOCKS
+#define IDW_BATCH_MIN_BLOCKS 6
+#endif
+
 template <int NB>
 struct BatchSmem {
     float sn[NB][3][128], cn[NB][3][128];  // this mirror's numerator pairs
@@ -39,7 +44,7 @@ __device__ __forceinline__ void flush_partials(BatchSmem<NB> &sm, float (&pn)[NB
 }
 
 template <int KIND, int NB>
-__global__ void __launch_bounds__(128, 6)
+__global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
     k_walk_mixed_batch(TreeDev t, TreeDevF tf, PointsDevF pf, int64_t ptStrideB, NodeAggF af, int64_t nodeStrideB,
                        int64_t dnStrideB, VolumeDev v, WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
                        float4 *acc, int64_t accStrideB, unsigned long long *counters) {
@@ -344,9 +349,13 @@ void launch_batch_kind(int nb, const TreeDev &t, const TreeDevF &tf, const Point
             launch_batch_nb<KIND, 3>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
                                      accStrideB, counters, st);
             break;
-        default:
+        case 4:
             launch_batch_nb<KIND, 4>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
                                      accStrideB, counters, st);
+            break;
+        default:
+            launch_batch_nb<KIND, kBatchMax>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact,
+                                             acc, accStrideB, counters, st);
             break;
     }
 }

@@ -23,6 +23,13 @@ struct TreeDev {
     const dbl4 *geom;  // X, oradius
     const double *err;    // 12 per node
     const double *ai;     // per node
+    const int *parent = nullptr;  // per node: parent index, -1 at the root
+};
+
+// Scratch of the bottom-up cluster sums: 12 doubles and one arrival counter per node.
+struct SetDataScratch {
+    double *sum;
+    unsigned *flags;
 };
 
 // Everything the mixed walks read at a tree node, packed in one 128-byte
@@ -111,7 +118,8 @@ void launch_corners(const SurfaceDev &s, const double *Xu, const double *normals
                     int *isCorner, cudaStream_t st);
 void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
                   const double *Ai, const int *isCorner, int useRotations, double *ptMB, cudaStream_t st);
-void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, cudaStream_t st);
+void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, const SetDataScratch &sc, cudaStream_t st);
+void launch_tree_parents(const TreeDev &t, int *parent, cudaStream_t st);
 void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st);
 void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
                     const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
@@ -152,7 +160,12 @@ int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeD
                              double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
                              unsigned long long *counters, cudaStream_t st);
 MixedParams make_mixed_params(const EvalConsts &k);
-// nb (1..4) surfaces in one mixed walk (idw_batch.cu): per-surface point and
+// Largest number of surfaces that share one batched walk.
+#ifndef IDW_BATCH_MAX
+#define IDW_BATCH_MAX 4
+#endif
+constexpr int kBatchMax = IDW_BATCH_MAX;
+// nb (1..kBatchMax) surfaces in one mixed walk (idw_batch.cu): per-surface point and
 // cluster arrays at strides ptStrideB / nodeStrideB / dnStrideB (floats), the
 // reference motions at af.ref + 24 b, accumulators at acc + accStrideB * b.
 void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, int64_t ptStrideB,

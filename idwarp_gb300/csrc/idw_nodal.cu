@@ -333,17 +333,18 @@ __global__ void k_nodal(SurfaceDev s, const double *Xu, const dbl4 *xa, const do
 }
 
 // setData: unweighted mean of the 12 node values over each interior node's
-// range (kd_tree.F90:595-617); one warp per node, lanes stride the range.
-__global__ void k_set_data(TreeDev t, const double *ptMB, double *nodeMB) {
-    const int q = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (q >= t.nNodes) return;
-    const int4 inf = t.info[q];
-    if (inf.w) return;  // leaves carry no aggregate
+// range (kd_tree.F90:595-617), bottom-up: a leaf sums its own points, and the
+// second child to finish adds the two child sums into the parent and carries
+// on towards the root (the first one stops).  Every point is read once.
+__global__ void k_set_data(TreeDev t, const double *ptMB, double *nodeMB, double *sum, unsigned *flags) {
+    const int q0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q0 >= t.nNodes) return;
+    const int4 inf = t.info[q0];
+    if (!inf.w) return;
     double acc[12];
 #pragma unroll
     for (int c = 0; c < 12; ++c) acc[c] = 0.0;
-    for (int i = inf.x + lane; i <= inf.y; i += 32) {
+    for (int i = inf.x; i <= inf.y; ++i) {
         const double2 *p = reinterpret_cast<const double2 *>(ptMB + 12 * i);
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
@@ -352,12 +353,35 @@ __global__ void k_set_data(TreeDev t, const double *ptMB, double *nodeMB) {
             acc[2 * c + 1] += v.y;
         }
     }
-    const double cnt = double(inf.y - inf.x + 1);
 #pragma unroll
-    for (int c = 0; c < 12; ++c) {
-        const double v = warp_sum(acc[c]);
-        if (lane == c) nodeMB[12 * q + c] = v / cnt;
+    for (int c = 0; c < 12; ++c) sum[12 * q0 + c] = acc[c];
+    int q = q0;
+    while (true) {
+        const int p = t.parent[q];
+        if (p < 0) break;
+        __threadfence();
+        if (atomicAdd(flags + p, 1u) == 0u) break;  // the sibling is not done yet
+        const int a = p + 1, b = t.info[a].z;
+        const int4 pi = t.info[p];
+        const double cnt = double(pi.y - pi.x + 1);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) {
+            const double s = __ldcg(sum + 12 * a + c) + __ldcg(sum + 12 * b + c);
+            sum[12 * p + c] = s;
+            nodeMB[12 * p + c] = s / cnt;
+        }
+        q = p;
     }
+}
+
+__global__ void k_tree_parents(TreeDev t, int *parent) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= t.nNodes) return;
+    if (q == 0) parent[0] = -1;
+    const int4 inf = t.info[q];
+    if (inf.w) return;
+    parent[q + 1] = q;
+    parent[t.info[q + 1].z] = q;
 }
 
 // setData_b: push the cluster adjoints down to the member points
@@ -612,8 +636,13 @@ void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const d
     if (s.n > 0)
         k_nodal<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, Ai, isCorner, useRotations, ptMB);
 }
-void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, cudaStream_t st) {
-    if (t.nNodes > 0) k_set_data<<<blocks(int64_t(t.nNodes) * 32, 128), 128, 0, st>>>(t, ptMB, nodeMB);
+void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, const SetDataScratch &sc, cudaStream_t st) {
+    if (t.nNodes <= 0) return;
+    cudaMemsetAsync(sc.flags, 0, sizeof(unsigned) * size_t(t.nNodes), st);
+    k_set_data<<<blocks(t.nNodes, 128), 128, 0, st>>>(t, ptMB, nodeMB, sc.sum, sc.flags);
+}
+void launch_tree_parents(const TreeDev &t, int *parent, cudaStream_t st) {
+    if (t.nNodes > 0) k_tree_parents<<<blocks(t.nNodes, 128), 128, 0, st>>>(t, parent);
 }
 void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st) {
     if (nPts > 0) k_set_data_b<<<blocks(nPts, 128), 128, 0, st>>>(t, nodeAdj, ptAdj, nPts);
