@@ -79,6 +79,9 @@ struct Ctx {
     DevBuf<double> bXs, bXu, bPtMB, bNodeMB;
     DevBuf<float> bPtDM, bPtDMl, bNodeDC, bNodeDCl, bNodeDn, bRef;
     DevBuf<float4> bAcc;
+    // warpDeriv accumulators (grown on demand)
+    int adjSeeds = 0;
+    DevBuf<double> adjPt, adjNode, adjRel;
     bool gdenValid = false;
     double gdenLdefFact = 0.0, gdenAlpha = 0.0;
     int gdenMode = -1;
@@ -165,6 +168,10 @@ WeightLaw make_init_law(const Ctx *c) {
     w.alphaToBexp = std::pow(c->optInit.alpha, c->optInit.bExp);
     return w;
 }
+
+struct DevView {
+    double *p;
+};
 
 TreeDev tree_dev(Ctx *c) {
     TreeDev t;
@@ -943,10 +950,16 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     const int n = c->nUnique, nn = c->nNodes;
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     const int mixed = c->opt.precision == IDW_PREC_MIXED;
-    DevBuf<double> ptAdj, nodeAdj, ptRel;
-    CKA(ptAdj.alloc(size_t(nSeeds) * 12 * n));
-    CKA(nodeAdj.alloc(size_t(nSeeds) * 12 * nn));
-    if (mixed) CKA(ptRel.alloc(size_t(nSeeds) * 12 * n));
+    // accumulators owned by the context (grown on demand): a call with device
+    // pointers and a seed count already seen allocates nothing, so it can be
+    // captured in a CUDA graph
+    if (c->adjSeeds < nSeeds) {
+        CKA(c->adjPt.alloc(size_t(nSeeds) * 12 * n));
+        CKA(c->adjNode.alloc(size_t(nSeeds) * 12 * nn));
+        CKA(c->adjRel.alloc(size_t(nSeeds) * 12 * n));
+        c->adjSeeds = nSeeds;
+    }
+    DevView ptAdj{c->adjPt.p}, nodeAdj{c->adjNode.p}, ptRel{c->adjRel.p};
     CK(cudaMemsetAsync(ptAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * n, c->stream));
     CK(cudaMemsetAsync(nodeAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * nn, c->stream));
     CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
@@ -1007,7 +1020,7 @@ int idw_warp_deriv(void *ctx, const double *dxv, int64_t ndof, int where) {
     }
     int rc = run_deriv(c, d, 1, ndof, c->dxs.p, IDW_DEVICE, 3 * int64_t(c->nPts));
     if (rc) return rc;
-    CK(cudaStreamSynchronize(c->stream));
+    if (where != IDW_DEVICE) CK(cudaStreamSynchronize(c->stream));
     c->haveDxs = true;
     return IDW_OK;
 }
@@ -1037,7 +1050,8 @@ int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *d
     }
     int rc = run_deriv(c, d, nseeds, int64_t(vdof), dxs, where, 3 * int64_t(c->nPts));
     if (rc) return rc;
-    CK(cudaStreamSynchronize(c->stream));
+    // host results were synchronised by the copies; device results are
+    // ordered on the stream
     return IDW_OK;
 }
 
