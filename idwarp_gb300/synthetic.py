@@ -186,3 +186,81 @@ def wing_perturbation(pts, seed=2, twist_tip_deg=-4.0, semispan=3.0, ffd=(8, 6, 
     dz = np.einsum("pi,pj,pk,ijk->p", Bu, Bv, Bw, ctrl)
     p[:, 2] += dz
     return p
+
+
+def sphere_cells(n, layers):
+    """Hexahedral cells (N, 8) of ``sphere_ogrid(n, layers)`` (volume node indices)."""
+    xi = np.tan(np.pi / 4 * np.linspace(-1.0, 1.0, n + 1))
+    m = sphere_ogrid(n=n, layers=1)
+    pts = m["pts"]
+    key = np.round(pts * 1e12).astype(np.int64)
+    _, first_idx, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    # volume nodes use the unique directions in order of first appearance
+    order = np.argsort(np.argsort(first_idx))
+    dir_of_pt = order[inv.ravel()]
+    nd = len(first_idx)
+    q = dir_of_pt[m["conn"].reshape(-1, 4)]
+    cells = []
+    for k in range(layers):
+        cells.append(np.concatenate([q + k * nd, q + (k + 1) * nd], axis=1))
+    del xi
+    return np.concatenate(cells).astype(np.int64)
+
+
+def wing_cells(ni, nj, nk):
+    """Hexahedral cells (N, 8) of ``wing_shell(ni, nj, nk)`` (volume node indices)."""
+    idx = np.arange(nk * nj * ni).reshape(nk, nj, ni)
+    a = idx[:-1, :-1, :-1]
+    b = idx[:-1, :-1, 1:]
+    c = idx[:-1, 1:, 1:]
+    d = idx[:-1, 1:, :-1]
+    e = idx[1:, :-1, :-1]
+    f = idx[1:, :-1, 1:]
+    g = idx[1:, 1:, 1:]
+    h = idx[1:, 1:, :-1]
+    return np.stack([a, b, c, d, e, f, g, h], axis=-1).reshape(-1, 8).astype(np.int64)
+
+
+def multibody(wing=(577, 261, 53), sphere=(158, 79), sphere_radius=0.5, sphere_center=(0.5, 4.5, 0.0),
+              sphere_far=10.0):
+    """Two bodies in one warp: the NACA0012 half-wing shell and a sphere O-grid
+    (radius ``sphere_radius`` at ``sphere_center``, beside the wing tip), one
+    surface definition and one volume point set (the two blocks overlap; IDW
+    needs no connectivity).  ``cells`` lists the hexahedra of both blocks.
+    Default sizes: 7.98M + 11.98M = 19.96M volume nodes, 150,597 + 151,686
+    surface points."""
+    ni, nj, nk = wing
+    n, layers = sphere
+    w = wing_shell(ni, nj, nk)
+    s = sphere_ogrid(n=n, layers=layers, r_out=sphere_far / sphere_radius)
+    c = np.asarray(sphere_center, dtype=np.float64)
+    s_xv0 = s["xv0"] * sphere_radius + c
+    s_pts = s["pts"] * sphere_radius + c
+    nwv, nwp = len(w["xv0"]), len(w["pts"])
+    cells = np.concatenate([wing_cells(ni, nj, nk), sphere_cells(n, layers) + nwv])
+    xv0 = np.concatenate([w["xv0"], s_xv0])
+    # orient every hexahedron so that its initial volume is positive
+    flip = hex_volumes_np(xv0, cells) < 0
+    cells[flip] = cells[flip][:, [4, 5, 6, 7, 0, 1, 2, 3]]
+    return {"xv0": xv0, "pts": np.concatenate([w["pts"], s_pts]),
+            "conn": np.concatenate([w["conn"], s["conn"] + nwp]).astype(np.intc),
+            "faceSizes": np.concatenate([w["faceSizes"], s["faceSizes"]]).astype(np.intc),
+            "symmetryPlanes": w["symmetryPlanes"], "cells": cells, "nWingPts": nwp,
+            "name": "multibody_wing%dx%dx%d_sphere%dx%d" % (ni, nj, nk, n, layers)}
+
+
+# six tetrahedra around the diagonal 0-6 of a hexahedron (corners 0-3 bottom,
+# 4-7 top, both counter-clockwise seen from below)
+HEX_TETS = ((0, 1, 2, 6), (0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 4, 5, 6), (0, 5, 1, 6))
+
+
+def hex_volumes_np(xv, cells, chunk=1 << 20):
+    """Signed volumes of hexahedra (sum of six tetrahedra), numpy."""
+    out = np.empty(len(cells))
+    for s0 in range(0, len(cells), chunk):
+        x = xv[cells[s0:s0 + chunk]]
+        v = 0.0
+        for a, b, c, d in HEX_TETS:
+            v = v + np.einsum("ij,ij->i", np.cross(x[:, b] - x[:, a], x[:, c] - x[:, a]), x[:, d] - x[:, a]) / 6.0
+        out[s0:s0 + chunk] = v
+    return out
