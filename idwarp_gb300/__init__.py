@@ -6,6 +6,7 @@ evaluation runs in hand-written sm_103a CUDA kernels behind the C ABI of
 """
 from .options import Error
 from .UnstructuredMesh import USMesh, pointReduce
+from .MultiUnstructuredMesh import MultiUSMesh
 
 __version__ = "0.1.0"
-__all__ = ["USMesh", "Error", "pointReduce"]
+__all__ = ["USMesh", "MultiUSMesh", "Error", "pointReduce"]
