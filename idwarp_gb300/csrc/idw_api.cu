@@ -645,6 +645,14 @@ int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int whe
     return copy_out(c, coords, c->xs.p, size_t(cdof), where);
 }
 
+// Threshold of the mixed walk's double-float terms: mixedGate * Ldef0 (the
+// motions are lengths: Ldef0, not the weight law's LdefFact-scaled L),
+// tightened beyond one symmetry plane, where every node sums nLoop mirror walks
+// of FP32 terms.
+static double mixed_gate(const Ctx *c) {
+    return c->opt.mixedGate * c->Ldef0 * std::min(1.0, 2.0 / double(std::max(1, c->sym.nLoop)));
+}
+
 // The mixed walk's precision gate wants each node's final denominator, which
 // depends on Xu0 and the weight law only (not on the surface coordinates):
 // one walk that keeps only the denominators, run once per law.
@@ -678,7 +686,7 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     k.sym = c->sym;
     k.slotStats = c->opt.diagnostics & 1;
     // terms whose weight x (motion + lever arm) exceeds mixedGate*Ldef*den0 are summed in double-float
-    k.precGate = c->opt.mixedGate * c->Ldef0 * c->opt.LdefFact;
+    k.precGate = mixed_gate(c);
     PointsDev p;
     p.xa = c->ptXA.p;
     p.mb = c->ptMB.p;
@@ -790,7 +798,7 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = 0;
-    k.precGate = c->opt.mixedGate * c->Ldef0 * c->opt.LdefFact;
+    k.precGate = mixed_gate(c);
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     TreeDevF tf;
     tf.nodes = c->nodeRec.p;

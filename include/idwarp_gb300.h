@@ -66,9 +66,10 @@ typedef struct idw_options {
     int32_t precision;    /* IDW_PREC_MIXED (default) or IDW_PREC_FP64 */
     int32_t diagnostics;  /* bit 0: count warp-level lane slots in idw_stats */
     double mixedGate;     /* mixed mode: a term w (|S'| + |D'| |r - X|) larger than
-                           * mixedGate * Ldef * denominator0 is summed in double-float
-                           * (S' = the term's motion less the mean surface motion;
-                           * default 2e-3; 0 = every term) */
+                           * mixedGate * Ldef0 * den (times 2/nLoop beyond one symmetry
+                           * plane) is summed in double-float (S' = the term's motion
+                           * less the mean surface motion, den = the node's
+                           * denominator; default 2e-3; 0 = every term) */
     int32_t reserved[4];
 } idw_options;
 

@@ -1,0 +1,98 @@
+"""Edge cases of the warping path on the GPU against the oracle: extreme
+options (LdefFact 100, exponents 4/6 overflow FP32 without scaling), several
+symmetry planes, bucket sizes, errTol 0, a one-leaf tree, rotations and corner
+handling switched off, non-finite and mismatched input."""
+import numpy as np
+import pytest
+
+from tests.meshes import OPTS, build_gpu, build_oracle, sphere_small, wing_small
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sphere():
+    return sphere_small()
+
+
+def _cmp(m, opts, sym=True, tol64=1e-12, tol32=1e-8, counts=True):
+    om = build_oracle(m, opts, sym=sym)
+    om.set_surface_coordinates(m["xs"])
+    xo = om.warp()
+    L = om.ldef0()
+    so = om.stats()
+    for precision, tol in (("fp64", tol64), ("mixed", tol32)):
+        g = build_gpu(m, opts, sym=sym, precision=precision)
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        err = np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / L
+        assert err < tol, (precision, opts, err)
+        if counts:
+            st = g.getStats()
+            assert st["leafPairs"] == so["leafPairs"], (precision, opts)
+            assert st["approx"] == so["approx"], (precision, opts)
+
+
+@pytest.mark.parametrize("opts", [{"LdefFact": 100.0}, {"LdefFact": 0.01}, {"aExp": 4.0, "bExp": 6.0},
+                                  {"alpha": 2.0}, {"alpha": 0.0}])
+def test_extreme_weight_laws(sphere, opts, built_lib, oracle_lib):
+    _cmp(sphere, opts)
+
+
+@pytest.mark.parametrize("bucket", [1, 4, 16, 64])
+def test_bucket_sizes(sphere, bucket, built_lib, oracle_lib):
+    _cmp(sphere, {"bucketSize": bucket})
+
+
+def test_errtol_zero_is_exact(sphere, built_lib, oracle_lib):
+    om = build_oracle(sphere, {"evalMode": "exact"})
+    om.set_surface_coordinates(sphere["xs"])
+    xe = om.warp()
+    g = build_gpu(sphere, {"errTol": 0.0}, precision="mixed")
+    g.setSurfaceCoordinates(sphere["xs"])
+    g.warpMesh()
+    assert g.getStats()["approx"] == 0
+    assert np.abs(g.getWarpGrid().reshape(-1, 3) - xe).max() / om.ldef0() < 1e-8
+
+
+def test_rotations_and_corners_off(built_lib, oracle_lib):
+    m = wing_small()
+    _cmp(m, {"useRotations": False})
+    _cmp(m, {"zeroCornerRotations": False})
+    _cmp(m, {"cornerAngle": 80.0})
+
+
+@pytest.mark.parametrize("nplanes", [2, 3])
+def test_several_symmetry_planes(nplanes, built_lib, oracle_lib):
+    # the sphere cut by planes through its centre: x = 0, y = 0, z = 0
+    m = dict(sphere_small())
+    planes = [[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], [[0.0, 0.0, 0.0], [0.0, 1.0, 0.0]],
+              [[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]]][:nplanes]
+    m["symmetryPlanes"] = planes
+    _cmp(m, {})
+
+
+def test_single_leaf_tree(built_lib, oracle_lib):
+    # a surface small enough that the root is a leaf: exact sums only
+    from idwarp_gb300 import synthetic as S
+
+    m = S.sphere_ogrid(n=1, layers=4)
+    m["xs"] = S.sphere_perturbation(m["pts"], seed=0)
+    _cmp(m, {"bucketSize": 64})
+
+
+def test_bad_input_raises(sphere, built_lib):
+    from idwarp_gb300 import Error
+    from idwarp_gb300._lib import LibraryError
+
+    g = build_gpu(sphere, precision="mixed")
+    with pytest.raises(Error):
+        g.setSurfaceCoordinates(np.full_like(sphere["xs"], np.inf))
+    with pytest.raises(Error):
+        g.setSurfaceCoordinates(sphere["xs"][:-2])
+    g.setSurfaceCoordinates(sphere["xs"])
+    g.warpMesh()
+    with pytest.raises(LibraryError):
+        g.warpDeriv(np.zeros(5), solverVec=False)
+    with pytest.raises(Error):
+        g.warpDerivFwd(np.zeros((3, 3)), solverVec=False)
