@@ -132,6 +132,7 @@ class USMesh(BaseSolver):
         n = x.shape[0]
         self._chk(self.lib.idw_create_common_grid(self.ctx, ptr, n, where), "createCommonGrid")
         self.nVol = n
+        self._gridSet = True
         self.warpInitialized = False
 
     # ------------------------------------------------------------------
@@ -193,7 +194,7 @@ class USMesh(BaseSolver):
         rng = np.arange(len(ind)).astype("intc")
         inv[ind[rng]] = rng
         link = np.ascontiguousarray(inv[link - 1] + 1, dtype=np.int32)
-        if self.nVol == 0:
+        if not getattr(self, "_gridSet", False):
             raise Error("The volume grid must be set (gridFile or createCommonGrid) before setSurfaceDefinition.")
         if self.getOption("restartFile") is not None:
             warnings.warn("restartFile is ignored: the denominator estimate is recomputed on the GPU.", stacklevel=2)

@@ -263,10 +263,11 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
                          const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st) {
-    if (v.nVol <= 0 || nSeeds <= 0) return 0;
+    if (nSeeds <= 0) return 0;
     const MixedParams mp = make_mixed_params(k);
     const int64_t ptStride = 12 * int64_t(nPts), nodeStride = 12 * int64_t(t.nNodes);
-    int s0 = 0;
+    // no volume nodes: no walk, the combination below writes zero adjoints
+    int s0 = v.nVol > 0 ? 0 : nSeeds;
     while (s0 < nSeeds) {
         const int left = nSeeds - s0;
         const double *d = dxv + s0 * dxvStride;

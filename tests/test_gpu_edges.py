@@ -96,3 +96,43 @@ def test_bad_input_raises(sphere, built_lib):
         g.warpDeriv(np.zeros(5), solverVec=False)
     with pytest.raises(Error):
         g.warpDerivFwd(np.zeros((3, 3)), solverVec=False)
+
+
+@pytest.mark.parametrize("opts,planes", [({"LdefFact": 100.0}, 0), ({}, 2)])
+def test_mixed_derivatives_extreme_cases(opts, planes, built_lib):
+    # reverse and tangent products of the mixed form against FP64 where the
+    # forward needed care (large LdefFact, several mirrors)
+    m = dict(sphere_small())
+    if planes:
+        m["symmetryPlanes"] = [[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]], [[0.0, 0.0, 0.0], [0.0, 1.0, 0.0]]][:planes]
+    rng = np.random.default_rng(51)
+    dxv = rng.normal(size=3 * len(m["xv0"]))
+    dxs = rng.normal(size=m["pts"].shape)
+    out = {}
+    for precision in ("fp64", "mixed"):
+        g = build_gpu(m, opts, precision=precision)
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        g.warpDeriv(dxv, solverVec=False)
+        out[precision] = (g.getdXs(), g.warpDerivFwd(dxs, solverVec=False))
+    for k in range(2):
+        ref = out["fp64"][k]
+        assert np.abs(out["mixed"][k] - ref).max() <= 1e-6 * np.abs(ref).max(), k
+
+
+def test_empty_volume_mesh(sphere, built_lib):
+    import contextlib
+    import io
+
+    from idwarp_gb300 import USMesh
+
+    o = dict(OPTS, fileType="NPY", precision="mixed")
+    with contextlib.redirect_stdout(io.StringIO()):
+        g = USMesh(options=o)
+        g.createCommonGrid(np.zeros((0, 3)))
+        g.setSurfaceDefinition(sphere["pts"], sphere["conn"], sphere["faceSizes"])
+    g.setSurfaceCoordinates(sphere["xs"])
+    g.warpMesh()
+    assert g.getWarpGrid().size == 0
+    g.warpDeriv(np.zeros(0), solverVec=False)
+    assert np.all(g.getdXs() == 0.0)
