@@ -550,6 +550,12 @@ def main():
                        "speedup_mixed_over_fp64": ms64 / ms_step,
                        "same_decisions": bool(s64["leafPairs"] == st["leafPairs"] and s64["approx"] == st["approx"]),
                        "max_err_over_Ldef": float(errv.max()), "rms_err_over_Ldef": float(np.sqrt(np.mean(errv ** 2)))}
+        # run-time launch shapes (surfaces per batched walk, seeds per adjoint
+        # walk) tuned on this mesh before the batched timings below
+        out["autotune"] = mesh.autotune(nSurfaces=8, nSeeds=16)
+        L.idw_set_stream(mesh.ctx, C.c_void_p(stream.cuda_stream))
+        mesh.setSurfaceCoordinates(xs_host)
+        mesh.warpMesh()
         # 16-seed reverse derivative sharing one walk: mixed (product) and FP64 plain form
         rng = np.random.default_rng(100)
         seeds = rng.normal(size=(16, nvol, 3))

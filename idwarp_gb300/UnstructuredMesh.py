@@ -356,6 +356,15 @@ class USMesh(BaseSolver):
                                                   C.c_void_p(out.ctypes.data), _lib.IDW_HOST), "warpDerivBatch")
         return out
 
+    def autotune(self, nSurfaces=8, nSeeds=16):
+        """Time the mixed form's run-time launch shapes (surfaces per batched
+        walk, seeds per adjoint walk) on this mesh and keep the fastest.
+        Warps the current surface first."""
+        self.warpMesh()
+        t = _lib.idw_tuning()
+        self._chk(self.lib.idw_autotune(self.ctx, int(nSurfaces), int(nSeeds), C.byref(t)), "autotune")
+        return t.as_dict()
+
     def getStats(self):
         """Work counters of the last warp/derivative call."""
         s = _lib.idw_stats()

@@ -53,6 +53,15 @@ class idw_stats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
 
 
+class idw_tuning(C.Structure):
+    _fields_ = [("batchGroup", C.c_int32), ("adjMaxGroup", C.c_int32), ("batchMs", C.c_double * 4),
+                ("adjMs", C.c_double * 3), ("reserved", C.c_int32 * 4)]
+
+    def as_dict(self):
+        return {"batchGroup": self.batchGroup, "adjMaxGroup": self.adjMaxGroup, "batchMs": list(self.batchMs),
+                "adjMs": dict(zip((16, 8, 4), list(self.adjMs)))}
+
+
 class LibraryError(RuntimeError):
     pass
 
@@ -91,6 +100,7 @@ _SIGS = {
     "idw_warp_deriv_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_warp_deriv_fwd": [_VP, _VP, C.c_int64, _VP, C.c_int64, C.c_int],
     "idw_warp_deriv_noalloc": [_VP, _VP, C.c_int64, _VP, C.c_int64],
+    "idw_autotune": [_VP, C.c_int32, C.c_int32, C.POINTER(idw_tuning)],
     "idw_get_denominator0": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_denominator": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_stats": [_VP, C.POINTER(idw_stats)],

@@ -262,7 +262,7 @@ void launch_adj_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, 
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
-                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st) {
+                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st, int maxGroup) {
     if (nSeeds <= 0) return 0;
     const MixedParams mp = make_mixed_params(k);
     const int64_t ptStride = 12 * int64_t(nPts), nodeStride = 12 * int64_t(t.nNodes);
@@ -272,11 +272,16 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
         const int left = nSeeds - s0;
         const double *d = dxv + s0 * dxvStride;
         double *pa = ptAcc + s0 * ptStride, *na = nodeAcc + s0 * nodeStride;
-        if (left >= 16) {
+        // seeds in groups of 16, 8, 4 or 1 sharing one walk, none above maxGroup
+        if (left >= 16 && maxGroup >= 16) {
             launch_adj_law<16>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
                                counters, st);
             s0 += 16;
-        } else if (left >= 4) {
+        } else if (left >= 8 && maxGroup >= 8) {
+            launch_adj_law<8>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
+                              counters, st);
+            s0 += 8;
+        } else if (left >= 4 && maxGroup >= 4) {
             launch_adj_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
                               counters, st);
             s0 += 4;

@@ -79,6 +79,9 @@ struct Ctx {
     DevBuf<double> bXs, bXu, bPtMB, bNodeMB;
     DevBuf<float> bPtDM, bPtDMl, bNodeDC, bNodeDCl, bNodeDn, bRef;
     DevBuf<float4> bAcc;
+    // tuned launch shapes (idw_autotune)
+    int batchGroup = kBatchMax;  // surfaces per batched walk
+    int adjMaxGroup = 16;        // seeds per adjoint walk
     // warpDeriv accumulators (grown on demand)
     int adjSeeds = 0;
     DevBuf<double> adjPt, adjNode, adjRel;
@@ -847,8 +850,9 @@ int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double 
             CKA(tin.alloc(size_t(g) * sdof));
             CKA(tout.alloc(size_t(g) * vdof));
         }
-        for (int b0 = 0; b0 < nbatch; b0 += kBatchWalk) {
-            const int nb = std::min<int>(kBatchWalk, nbatch - b0);
+        const int G = std::max(1, std::min(c->batchGroup, kBatchWalk));
+        for (int b0 = 0; b0 < nbatch; b0 += G) {
+            const int nb = std::min<int>(G, nbatch - b0);
             const double *cin = coords + size_t(b0) * sdof;
             double *cout = out + size_t(b0) * vdof;
             if (where != IDW_DEVICE) {
@@ -984,7 +988,7 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
         launch_adjoint_mixed(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride, c->den.p,
-                             ptAdj.p, nodeAdj.p, ptRel.p, c->ptXA.p, n, c->counters.p, c->stream);
+                             ptAdj.p, nodeAdj.p, ptRel.p, c->ptXA.p, n, c->counters.p, c->stream, c->adjMaxGroup);
     } else {
         launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride,
                                  ptAdj.p, nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
@@ -1430,6 +1434,105 @@ int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *d
     CK(cudaMemsetAsync(dxs, 0, sizeof(double) * size_t(cdof), c->stream));
     launch_scatter_dxs(n, c->xuInd.p, c->xub.p, dxs, c->stream);
     return check_launch(c, "reverse nodal properties");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// A small autotuner for the two launch shapes that are free at run time: the
+// number of surfaces that share one batched walk and the number of seeds that
+// share one adjoint walk.  Each candidate is timed once (after one warm-up) on
+// the context's own mesh and current surface.
+namespace {
+__global__ void k_fill(int64_t n, double v, double *x) {
+    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v * double(1 + (i % 7));
+}
+}  // namespace
+
+extern "C" {
+
+int idw_autotune(void *ctx, int32_t nsurfaces, int32_t nseeds, idw_tuning *out) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before idw_autotune");
+    if (nsurfaces < 1 || nseeds < 1 || !out) return fail(c, IDW_ERR_ARG, "bad autotune arguments");
+    if (c->opt.precision != IDW_PREC_MIXED) return fail(c, IDW_ERR_STATE, "the tuned launches are the mixed ones");
+    CK(cudaSetDevice(c->device));
+    std::memset(out, 0, sizeof(*out));
+    const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto timed = [&](auto &&fn, float &ms) -> int {
+        int rc = fn();  // warm-up (and growth of any buffers)
+        if (rc) return rc;
+        CK(cudaEventRecord(e0, c->stream));
+        rc = fn();
+        if (rc) return rc;
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        return IDW_OK;
+    };
+    int rc = IDW_OK;
+    {
+        // batched walk: the current surface, nsurfaces times
+        DevBuf<double> xs, xv;
+        CKA(xs.alloc(size_t(nsurfaces) * sdof));
+        CKA(xv.alloc(size_t(kBatchMax) * vdof));
+        for (int b = 0; b < nsurfaces; ++b)
+            CK(cudaMemcpyAsync(xs.p + size_t(b) * sdof, c->xs.p, sdof * sizeof(double), cudaMemcpyDeviceToDevice,
+                               c->stream));
+        float best = 0.f;
+        for (int G = 1; G <= kBatchMax && G <= 4; ++G) {
+            float ms = 0.f;
+            rc = timed([&]() {
+                for (int b0 = 0; b0 < nsurfaces; b0 += G) {
+                    const int nb = std::min(G, nsurfaces - b0);
+                    int r = run_warp_batch_mixed(c, xs.p + size_t(b0) * sdof, nb, xv.p);
+                    if (r) return r;
+                }
+                return int(IDW_OK);
+            }, ms);
+            if (rc) break;
+            out->batchMs[G - 1] = ms;
+            if (G == 1 || ms < best) {
+                best = ms;
+                out->batchGroup = G;
+            }
+        }
+    }
+    if (!rc) {
+        // adjoint: seed groups of at most 16, 8 or 4
+        DevBuf<double> seeds, dxs;
+        CKA(seeds.alloc(size_t(nseeds) * vdof));
+        CKA(dxs.alloc(size_t(nseeds) * sdof));
+        const int64_t nd = int64_t(nseeds) * int64_t(vdof);
+        if (nd > 0) k_fill<<<int((nd + 255) / 256), 256, 0, c->stream>>>(nd, 1e-3, seeds.p);
+        const int groups[3] = {16, 8, 4};
+        float best = 0.f;
+        const int keep = c->adjMaxGroup;
+        for (int q = 0; q < 3; ++q) {
+            c->adjMaxGroup = groups[q];
+            float ms = 0.f;
+            rc = timed([&]() { return run_deriv(c, seeds.p, nseeds, int64_t(vdof), dxs.p, IDW_DEVICE, int64_t(sdof)); },
+                       ms);
+            if (rc) break;
+            out->adjMs[q] = ms;
+            if (q == 0 || ms < best) {
+                best = ms;
+                out->adjMaxGroup = groups[q];
+            }
+        }
+        c->adjMaxGroup = rc ? keep : out->adjMaxGroup;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    c->batchGroup = out->batchGroup;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
 }
 
 }  // extern "C"

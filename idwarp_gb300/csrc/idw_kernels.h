@@ -177,7 +177,8 @@ void launch_finalize_mixed(const VolumeDev &v, const WalkRecF &rec, const float4
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
-                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st);
+                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st,
+                         int maxGroup = 16);
 int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
                 cudaStream_t st);
 

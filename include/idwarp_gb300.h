@@ -228,6 +228,21 @@ int idw_get_surface_state(void *ctx, double *xu0, double *ai, double *normals0, 
  * current surface (computeNodalProperties, kd_tree.F90:1580-1664). */
 int idw_get_nodal_properties(void *ctx, double *mi, double *bi);
 
+/* Launch shapes chosen by idw_autotune, and the candidates' times. */
+typedef struct idw_tuning {
+    int32_t batchGroup;  /* surfaces per batched walk (1..4) */
+    int32_t adjMaxGroup; /* largest seed group per adjoint walk (16, 8 or 4) */
+    double batchMs[4];   /* nsurfaces warps with 1..4 surfaces per walk */
+    double adjMs[3];     /* nseeds reverse products with groups of 16, 8, 4 */
+    int32_t reserved[4];
+} idw_tuning;
+
+/* Time the run-time launch shapes of the mixed form on this context's mesh
+ * and current surface (nsurfaces surfaces for idw_warp_mesh_batch, nseeds
+ * seeds for idw_warp_deriv_batch) and keep the fastest for later calls.
+ * Needs a prior idw_warp_mesh in mixed precision.  No reference counterpart. */
+int idw_autotune(void *ctx, int32_t nsurfaces, int32_t nseeds, idw_tuning *out);
+
 /* Diagnostic: measured FP32 FFMA throughput of the current device (TFLOP/s),
  * the denominator of the mixed walk's roofline.  No reference counterpart. */
 int idw_probe_ffma(void *stream, int device, double *tflops);

@@ -337,3 +337,23 @@ def test_mixed_batch_walk_matches_fp64(case, mode, sphere, wing, built_lib):
     s64 = g64.getStats()
     assert st["leafPairs"] == 2 * s64["leafPairs"]
     assert st["approx"] == 2 * s64["approx"]
+
+
+def test_autotune_keeps_results(wing, built_lib):
+    from idwarp_gb300 import synthetic as S
+
+    g = build_gpu(wing, precision="mixed")
+    g.setSurfaceCoordinates(wing["xs"])
+    g.warpMesh()
+    surfaces = np.stack([S.wing_perturbation(wing["pts"], seed=60 + i) for i in range(3)])
+    seeds = np.random.default_rng(61).normal(size=(5,) + wing["xv0"].shape)
+    before = (g.warpMeshBatch(surfaces), g.warpDerivBatch(seeds))
+    t = g.autotune(nSurfaces=3, nSeeds=5)
+    assert t["batchGroup"] in (1, 2, 3, 4) and t["adjMaxGroup"] in (16, 8, 4)
+    assert all(ms > 0 for ms in t["batchMs"][:3])
+    g.setSurfaceCoordinates(wing["xs"])
+    g.warpMesh()
+    after = (g.warpMeshBatch(surfaces), g.warpDerivBatch(seeds))
+    L = g.getStats()["Ldef0"]
+    assert np.abs(after[0] - before[0]).max() / L < 1e-9
+    assert np.abs(after[1] - before[1]).max() <= 1e-6 * np.abs(before[1]).max()
