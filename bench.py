@@ -189,6 +189,19 @@ def run_cpu_baseline(m, budget_s=15.0, threads=None, seed=0):
                 n, nvol, ERR_TOL, dt)}
 
 
+def replica_throughput(ms_step, units_per_rank, world, device):
+    """Whole-job throughput of ``world`` replicas that each processed
+    ``units_per_rank`` units per step: the step time is the maximum over the
+    ranks (all-reduce MAX when a process group is up).  Returns (max ms, units/s)."""
+    import torch
+
+    t = torch.tensor([float(ms_step)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    return ms_max, world * units_per_rank / (ms_max * 1e-3)
+
+
 def _timed(fn, reps, stream):
     import torch
 
@@ -467,11 +480,7 @@ def main():
     st = mesh.getStats()
     kernel_ms = st["lastKernelMs"]
     ms_step = ms_total / args.steps
-    t = torch.tensor([ms_step], device="cuda")
-    if dist_on:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_step_max = float(t.item())
-    value = world * nvol / (ms_step_max * 1e-3)
+    ms_step_max, value = replica_throughput(ms_step, nvol, world, "cuda")
 
     # end-to-end through the public API with host buffers
     xs_host = np.ascontiguousarray(m["xs"])
@@ -487,10 +496,7 @@ def main():
         grid = mesh.getWarpGrid()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    te = torch.tensor([e2e_s], device="cuda")
-    if dist_on:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = world * nvol / float(te.item())
+    _, e2e_value = replica_throughput(e2e_s * 1e3, nvol, world, "cuda")
 
     out = {
         "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
