@@ -137,8 +137,6 @@ void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v,
                          const SymPlanes &sym, double *den0, cudaStream_t st);
 void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,
                          unsigned long long *codes, int *idx, cudaStream_t st);
-void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, const double *nodeX,
-                         float4 *ptDA, cudaStream_t st);
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
                         float *ptDM, float *ptDMl, cudaStream_t st);
 void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
@@ -152,7 +150,6 @@ void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, 
 void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
                        const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
                        const WalkOut &o, cudaStream_t st);
-void launch_to_float(int64_t n, const double *src, float *dst, cudaStream_t st);
 // Per node (Morton order): the scaled denominator of the last mixed walk (acc).
 void launch_gate_den(int64_t nVol, const float4 *acc, float *gden, cudaStream_t st);
 int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,

@@ -182,23 +182,6 @@ __global__ void k_morton(int64_t n, const double *xv0, double lo0, double lo1, d
     idx[i] = int(i);
 }
 
-// Point offsets from the centroid of their leaf (set-up constant, FP32).
-__global__ void k_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *geom, const dbl4 *ptXA,
-                               float4 *ptDA) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int q = 0;
-    while (q < nNodes) {
-        int4 inf = info[q];
-        if (inf.w) break;
-        int4 li = info[q + 1];
-        q = (i <= li.y) ? q + 1 : li.z;
-    }
-    dbl4 g = geom[q];
-    dbl4 x = ptXA[i];
-    ptDA[i] = make_float4(float(x.x - g.x), float(x.y - g.y), float(x.z - g.z), float(x.w));
-}
-
 // Reference motion of the mixed walk: Dref = Mbar - I and bref = bbar of the
 // root cluster (the mean over all surface points), or zero when the root is a
 // leaf.  The walk sums S - Sref(r) in FP32, where Sref(r) = Dref r + bref, and
@@ -298,18 +281,11 @@ __global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, const double *ptM
     nodeDn[q] = float(dn);
 }
 
-__global__ void k_to_float(int64_t n, const double *src, float *dst) {
-    int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = float(src[i]);
-}
 
 inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 
 }  // namespace
 
-void launch_to_float(int64_t n, const double *src, float *dst, cudaStream_t st) {
-    if (n > 0) k_to_float<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
-}
 
 void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err,
                            double *scratch, int64_t scratchLen, cudaStream_t st) {
@@ -362,12 +338,6 @@ void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, cons
         k_morton<<<blocks(nVol, 256), 256, 0, st>>>(nVol, xv0, lo[0], lo[1], lo[2], s[0], s[1], s[2], codes, idx);
 }
 
-void launch_mixed_points(int n, const int4 *info, int nNodes, const dbl4 *ptXA, const double *nodeX,
-                         float4 *ptDA, cudaStream_t st) {
-    if (n > 0)
-        k_mixed_points<<<blocks(n, 256), 256, 0, st>>>(n, info, nNodes, reinterpret_cast<const dbl4 *>(nodeX),
-                                                        ptXA, ptDA);
-}
 
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
                         float *ptDM, float *ptDMl, cudaStream_t st) {
