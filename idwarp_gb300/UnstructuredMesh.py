@@ -114,7 +114,9 @@ class USMesh(BaseSolver):
         elif self.fileType == "PLOT3D":
             from .plot3d import readPlot3D
 
-            self.createCommonGrid(readPlot3D(fileName))
+            nodes, sizes = readPlot3D(fileName, return_blocks=True)
+            self._plot3dShape = sizes  # writeGrid writes the same blocks back
+            self.createCommonGrid(nodes)
         elif self.fileType == "CGNS":
             raise Error(
                 "CGNS grid files need libcgns/HDF5, which this build does not link. Pass the volume nodes with "

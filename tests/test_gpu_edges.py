@@ -136,3 +136,32 @@ def test_empty_volume_mesh(sphere, built_lib):
     assert g.getWarpGrid().size == 0
     g.warpDeriv(np.zeros(0), solverVec=False)
     assert np.all(g.getdXs() == 0.0)
+
+
+def test_plot3d_grid_file_roundtrip(tmp_path, built_lib):
+    # a two-block PLOT3D volume grid in, warped grid out with the same blocks
+    import contextlib
+    import io
+
+    from idwarp_gb300 import USMesh
+    from idwarp_gb300 import synthetic as S
+    from idwarp_gb300.plot3d import readPlot3D, writePlot3D
+
+    m = S.wing_shell(ni=17, nj=7, nk=6, first=1e-3, far=5.0)
+    n = len(m["xv0"])
+    half = (n // 2) // (17 * 7) * (17 * 7)
+    sizes = np.array([[17, 7, half // (17 * 7)], [17, 7, (n - half) // (17 * 7)]])
+    f = tmp_path / "vol.xyz"
+    writePlot3D(str(f), m["xv0"], sizes)
+    o = dict(OPTS, fileType="PLOT3D", gridFile=str(f), precision="mixed", symmetryPlanes=m["symmetryPlanes"])
+    with contextlib.redirect_stdout(io.StringIO()):
+        g = USMesh(options=o)
+        g.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
+    xs = S.wing_perturbation(m["pts"], seed=2)
+    g.setSurfaceCoordinates(xs)
+    g.warpMesh()
+    out = tmp_path / "warped.xyz"
+    g.writeGrid(str(out))
+    back, sz = readPlot3D(str(out), return_blocks=True)
+    np.testing.assert_array_equal(sz, sizes)
+    np.testing.assert_array_equal(back, g.getCommonGrid().reshape(-1, 3))
