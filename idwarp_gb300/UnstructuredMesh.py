@@ -433,6 +433,11 @@ class USMesh(BaseSolver):
         else:
             raise Error("writeGrid supports the NPY and PLOT3D file types in this build.")
 
+    def writeOFGridTecplot(self, fileName):
+        """OpenFOAM grids (idwarp/UnstructuredMesh.py writeOFGridTecplot) need pyofm, which this build does
+        not use; write the grid with writeGrid (NPY or PLOT3D) instead."""
+        raise Error("writeOFGridTecplot needs an OpenFOAM grid (pyofm), which this build does not read.")
+
     # ------------------------------------------------------------------
     # internals
     # ------------------------------------------------------------------
