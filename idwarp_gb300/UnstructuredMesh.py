@@ -238,9 +238,14 @@ class USMesh(BaseSolver):
                                                      _lib.IDW_HOST), "warp_to_solver_grid")
         return solverGrid
 
-    def getWarpGrid(self):
-        """Current grid in warp order, flat (3*nVol,)."""
-        out = np.zeros(3 * self.nVol, self.dtype)
+    def getWarpGrid(self, out=None):
+        """Current grid in warp order, flat (3*nVol,).  ``out`` (optional) is a
+        contiguous float64 host array of that size to fill, e.g. in pinned
+        memory for fast repeated reads."""
+        if out is None:
+            out = np.zeros(3 * self.nVol, self.dtype)
+        elif out.dtype != np.float64 or out.size != 3 * self.nVol or not out.flags.c_contiguous:
+            raise Error("getWarpGrid(out=...) needs a contiguous float64 array of %d entries." % (3 * self.nVol))
         self._chk(self.lib.idw_get_volume_coordinates(self.ctx, C.c_void_p(out.ctypes.data), out.size,
                                                         _lib.IDW_HOST), "getWarpGrid")
         return out
