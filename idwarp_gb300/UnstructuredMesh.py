@@ -355,6 +355,16 @@ class USMesh(BaseSolver):
                                                  C.c_void_p(out.ctypes.data), _lib.IDW_HOST), "warpMeshBatch")
         return out
 
+    def warpDerivFwdBatch(self, dXs):
+        """Tangent products for several directions at the current surface (a
+        prior warpMesh is needed): dXs (D, nSurf, 3) -> dXv (D, nVol, 3) in
+        warp order."""
+        dXs = np.ascontiguousarray(dXs, dtype=np.float64).reshape(-1, self.nSurf, 3)
+        out = np.zeros((dXs.shape[0], self.nVol, 3))
+        self._chk(self.lib.idw_warp_deriv_fwd_batch(self.ctx, C.c_void_p(dXs.ctypes.data), dXs.shape[0],
+                                                    C.c_void_p(out.ctypes.data), _lib.IDW_HOST), "warpDerivFwdBatch")
+        return out
+
     def warpDerivBatch(self, dXv):
         """S reverse products at once: dXv (S, nVol, 3) in warp order -> dXs (S, nSurf, 3)."""
         dXv = np.ascontiguousarray(dXv, dtype=np.float64).reshape(-1, self.nVol, 3)

@@ -99,6 +99,7 @@ _SIGS = {
     "idw_get_dxs": [_VP, _VP, C.c_int64, C.c_int],
     "idw_warp_deriv_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_warp_deriv_fwd": [_VP, _VP, C.c_int64, _VP, C.c_int64, C.c_int],
+    "idw_warp_deriv_fwd_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_warp_deriv_noalloc": [_VP, _VP, C.c_int64, _VP, C.c_int64],
     "idw_autotune": [_VP, C.c_int32, C.c_int32, C.POINTER(idw_tuning)],
     "idw_get_denominator0": [_VP, _VP, C.c_int64, C.c_int],

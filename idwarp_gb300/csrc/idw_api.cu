@@ -765,7 +765,11 @@ int idw_warp_mesh(void *ctx) {
 // and a finalisation per surface.  coords/out are device pointers.
 static constexpr int kBatchWalk = kBatchMax;
 
-static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double *outDev) {
+// tangent = 1: coordsDev holds surface tangents dXs; the walk then uses the
+// tangent nodal properties (Md + I, bd) at the current surface and writes
+// dXv = num / den (warpDerivFwd for nb directions), gated by tangentGate.
+static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double *outDev, int tangent = 0,
+                                double tangentGate = 0.0) {
     const int n = c->nUnique, nn = c->nNodes;
     const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
     if (c->batchCap < nb) {
@@ -783,11 +787,17 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
         c->batchCap = kBatchWalk;
     }
     SurfaceDev s = surf_dev(c);
+    if (tangent) launch_gather_xu(n, c->xuInd.p, c->xs.p, c->xu.p, c->stream);
     for (int b = 0; b < nb; ++b) {
         double *xu = c->bXu.p + size_t(b) * 3 * n, *mb = c->bPtMB.p + size_t(b) * 12 * n;
         double *nmb = c->bNodeMB.p + size_t(b) * 12 * nn;
         launch_gather_xu(n, c->xuInd.p, coordsDev + size_t(b) * sdof, xu, c->stream);
-        launch_nodal(s, xu, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, mb, c->stream);
+        if (tangent)
+            launch_nodal_d(s, c->xu.p, xu, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, 1,
+                           mb, c->stream);
+        else
+            launch_nodal(s, xu, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, mb,
+                         c->stream);
         launch_set_data(tree_dev(c), mb, nmb, setdata_scratch(c), c->stream);
         launch_mixed_nodal(n, tree_dev(c), nmb, c->ptXA.p, mb, c->bPtDM.p + size_t(b) * 12 * n,
                            c->bPtDMl.p + size_t(b) * 12 * n, c->stream);
@@ -801,7 +811,7 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = 0;
-    k.precGate = mixed_gate(c);
+    k.precGate = tangent ? tangentGate : mixed_gate(c);
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     TreeDevF tf;
     tf.nodes = c->nodeRec.p;
@@ -826,7 +836,7 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
                             rec, k, exact, c->bAcc.p, 2 * c->nVol, c->counters.p, c->stream);
     for (int b = 0; b < nb; ++b)
         launch_finalize_mixed(vol_dev(c), rec, c->bAcc.p + size_t(b) * 2 * c->nVol, k.law.bExp,
-                              outDev + size_t(b) * vdof, c->stream);
+                              outDev + size_t(b) * vdof, c->stream, tangent);
     CK(cudaEventRecord(c->ev1, c->stream));
     c->eventsRecorded = true;
     return check_launch(c, "batch walk");
@@ -1531,6 +1541,66 @@ int idw_autotune(void *ctx, int32_t nsurfaces, int32_t nseeds, idw_tuning *out) 
     cudaEventDestroy(e1);
     if (rc) return rc;
     c->batchGroup = out->batchGroup;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// warpDerivFwd for several tangent directions: in mixed precision up to four
+// directions share one walk (the weights do not depend on the surface), in
+// FP64 one walk per direction.
+extern "C" {
+
+int idw_warp_deriv_fwd_batch(void *ctx, const double *dxs, int32_t ndir, double *dxv, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDerivFwd");
+    if (ndir < 0 || !dxs || !dxv) return fail(c, IDW_ERR_ARG, "bad tangent arguments");
+    CK(cudaSetDevice(c->device));
+    const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
+    if (where != IDW_DEVICE && !all_finite(dxs, size_t(ndir) * sdof))
+        return fail(c, IDW_ERR_NONFINITE, "non-finite dXs");
+    const int G = c->opt.precision == IDW_PREC_MIXED ? std::max(1, std::min(c->batchGroup, kBatchWalk)) : 1;
+    DevBuf<double> tin, tout;
+    if (where != IDW_DEVICE) {
+        CKA(tin.alloc(size_t(std::min<int>(ndir, G)) * sdof));
+        CKA(tout.alloc(size_t(std::min<int>(ndir, G)) * vdof));
+    }
+    for (int b0 = 0; b0 < ndir; b0 += G) {
+        const int nb = std::min(G, int(ndir) - b0);
+        const double *in = dxs + size_t(b0) * sdof;
+        double *out = dxv + size_t(b0) * vdof;
+        if (where != IDW_DEVICE) {
+            int rc = copy_in(c, tin.p, in, size_t(nb) * sdof, IDW_HOST);
+            if (rc) return rc;
+            in = tin.p;
+            out = tout.p;
+        }
+        int rc;
+        if (c->opt.precision == IDW_PREC_MIXED) {
+            // the gate scales with the largest tangent of the group
+            CK(cudaMemsetAsync(c->counters.p + 7, 0, sizeof(unsigned long long), c->stream));
+            const int64_t nd = int64_t(nb) * int64_t(sdof);
+            k_absmax<<<int((nd + 255) / 256), 256, 0, c->stream>>>(nd, in, c->counters.p + 7);
+            unsigned long long bits = 0;
+            CK(cudaMemcpyAsync(&bits, c->counters.p + 7, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+            double scale;
+            std::memcpy(&scale, &bits, sizeof(scale));
+            CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+            rc = run_warp_batch_mixed(c, in, nb, out, 1, c->opt.mixedGate * scale);
+        } else {
+            rc = run_deriv_fwd(c, in, out);
+        }
+        if (rc) return rc;
+        if (where != IDW_DEVICE) {
+            rc = copy_out(c, dxv + size_t(b0) * vdof, tout.p, size_t(nb) * vdof, IDW_HOST);
+            if (rc) return rc;
+        }
+    }
     CK(cudaStreamSynchronize(c->stream));
     return IDW_OK;
 }

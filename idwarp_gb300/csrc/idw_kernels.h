@@ -170,7 +170,7 @@ void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const
                              const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc, int64_t accStrideB,
                              unsigned long long *counters, cudaStream_t st);
 void launch_finalize_mixed(const VolumeDev &v, const WalkRecF &rec, const float4 *acc, double bExp, double *xv,
-                           cudaStream_t st);
+                           cudaStream_t st, int tangent = 0);
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,

@@ -307,8 +307,8 @@ inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 }  // namespace
 
 void launch_finalize_mixed(const VolumeDev &v, const WalkRecF &rec, const float4 *acc, double bExp, double *xv,
-                           cudaStream_t st) {
-    if (v.nVol > 0) k_finalize_mixed<<<blocks(v.nVol, 256), 256, 0, st>>>(v, rec, acc, bExp, 0, xv, nullptr);
+                           cudaStream_t st, int tangent) {
+    if (v.nVol > 0) k_finalize_mixed<<<blocks(v.nVol, 256), 256, 0, st>>>(v, rec, acc, bExp, tangent, xv, nullptr);
 }
 
 void launch_gate_den(int64_t nVol, const float4 *acc, float *gden, cudaStream_t st) {

@@ -190,6 +190,12 @@ int idw_warp_deriv_batch(void *ctx, const double *dxv, int32_t nseeds, double *d
  * is divided by that warp's denominator. */
 int idw_warp_deriv_fwd(void *ctx, const double *dxs, int64_t cdof, double *dxv, int64_t ndof, int where);
 
+/* idw_warp_deriv_fwd for ndir tangent directions: dxs holds ndir stacked
+ * (npts,3) tangents, dxv receives ndir stacked (nvol,3) products.  In mixed
+ * precision up to four directions share one tree walk.  No reference
+ * counterpart (the reference takes one direction per call). */
+int idw_warp_deriv_fwd_batch(void *ctx, const double *dxs, int32_t ndir, double *dxv, int where);
+
 /* idw_warp_deriv for one seed without allocating device memory in the call,
  * for callers that cannot allocate while they run (memory reserved up front,
  * allocation-free solver loops).  No reference counterpart.  dxv (nvol,3)

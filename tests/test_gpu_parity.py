@@ -357,3 +357,21 @@ def test_autotune_keeps_results(wing, built_lib):
     L = g.getStats()["Ldef0"]
     assert np.abs(after[0] - before[0]).max() / L < 1e-9
     assert np.abs(after[1] - before[1]).max() <= 1e-6 * np.abs(before[1]).max()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 1e-7)])
+def test_tangent_batch_matches_single(precision, tol, wing, built_lib):
+    # five directions: one shared walk of four, then one of one (mixed)
+    g = build_gpu(wing, precision=precision)
+    g.setSurfaceCoordinates(wing["xs"])
+    g.warpMesh()
+    rng = np.random.default_rng(71)
+    dirs = rng.normal(size=(5,) + wing["pts"].shape)
+    batch = g.warpDerivFwdBatch(dirs)
+    for d in range(5):
+        single = g.warpDerivFwd(dirs[d], solverVec=False).reshape(-1, 3)
+        assert np.abs(batch[d] - single).max() <= tol * np.abs(single).max(), d
+    # the warp itself is untouched
+    x = g.getWarpGrid()
+    g.warpMesh()
+    np.testing.assert_array_equal(g.getWarpGrid(), x)
