@@ -61,11 +61,14 @@ def mesh_options(m, precision, mode="fast"):
             "symmetryPlanes": m["symmetryPlanes"]}
 
 
-def build_mesh(m, precision, mode="fast"):
+def build_mesh(m, precision, mode="fast", restartFile=None):
     from idwarp_gb300 import USMesh
 
+    o = dict(mesh_options(m, precision, mode))
+    if restartFile:
+        o["restartFile"] = restartFile
     with contextlib.redirect_stdout(io.StringIO()):
-        mesh = USMesh(options=mesh_options(m, precision, mode))
+        mesh = USMesh(options=o)
         mesh.createCommonGrid(m["xv0"])
         mesh.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
     return mesh
@@ -629,6 +632,24 @@ def main():
                                 "ms": msb, "ms_per_surface": msb / 8, "speedup_per_surface_over_single": ms_step * 8 / msb,
                                 "max_err_over_Ldef_vs_fp64": float(errb)}
         del sb, ob
+        # set-up with a restart file: the first build computes the estimate
+        # and the dryRun costs and saves them, the next one loads and checks
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as td:
+            rf = os.path.join(td, "wing.restart")
+            t0 = time.perf_counter()
+            mr = build_mesh(m, "mixed", restartFile=rf)
+            t_first = time.perf_counter() - t0
+            first = mr.restartStatus
+            del mr
+            t0 = time.perf_counter()
+            mr = build_mesh(m, "mixed", restartFile=rf)
+            t_loaded = time.perf_counter() - t0
+            out["restart"] = {"setup_s_without": setup_s, "setup_s_first": t_first, "first": first,
+                              "setup_s_loaded": t_loaded, "loaded": mr.restartStatus,
+                              "file_bytes": os.path.getsize(rf)}
+            del mr
 
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = run_cpu_baseline(m)

@@ -12,7 +12,6 @@ run independent replicas, each with its own mesh object.
 """
 import ctypes as C
 import os
-import warnings
 
 import numpy as np
 
@@ -198,8 +197,6 @@ class USMesh(BaseSolver):
         link = np.ascontiguousarray(inv[link - 1] + 1, dtype=np.int32)
         if not getattr(self, "_gridSet", False):
             raise Error("The volume grid must be set (gridFile or createCommonGrid) before setSurfaceDefinition.")
-        if self.getOption("restartFile") is not None:
-            warnings.warn("restartFile is ignored: the denominator estimate is recomputed on the GPU.", stacklevel=2)
         self._setMeshOptions()
         self._chk(
             self.lib.idw_initialize_warping(self.ctx, _lib.dptr(allPts), len(allPts), _lib.dptr(uniquePts), nUnique,
@@ -208,7 +205,45 @@ class USMesh(BaseSolver):
             "setSurfaceDefinition")
         self.nSurf = len(pts)
         self.faceSizes = allFaceSizes
+        self.restartStatus = self._setDenominator0(self.getOption("restartFile"))
         self.warpInitialized = True
+
+    def _setDenominator0(self, restartFile):
+        """The denominator estimate: computed now, or through the restart file
+        (initializeWarping.F90:98-312; format in idwarp_gb300.restart)."""
+        if not restartFile:
+            self._chk(self.lib.idw_compute_denominator0(self.ctx), "denominator0")
+            return "computed"
+        from .restart import CHECK_STRIDE, load_or_compute
+
+        def load(den0):
+            rc = self.lib.idw_set_denominator0(self.ctx, C.c_void_p(den0.ctypes.data), den0.size, CHECK_STRIDE, _lib.IDW_HOST)
+            if rc in (_lib.IDW_ERR_RESTART, _lib.IDW_ERR_NONFINITE):
+                return False
+            self._chk(rc, "restartFile")
+            return True
+
+        def save():
+            den0 = np.zeros(self.nVol)
+            costs = np.zeros(self.nVol)
+            self._chk(self.lib.idw_get_denominator0(self.ctx, C.c_void_p(den0.ctypes.data), self.nVol, _lib.IDW_HOST),
+                      "denominator0")
+            self._chk(self.lib.idw_dry_run_costs(self.ctx, C.c_void_p(costs.ctypes.data), self.nVol, _lib.IDW_HOST), "dryRun")
+            return den0, costs
+
+        def compute():
+            self._chk(self.lib.idw_compute_denominator0(self.ctx), "denominator0")
+
+        log = print if self.comm.rank == 0 else (lambda *a: None)
+        return load_or_compute(restartFile, self.nVol, load, compute, save, log=log)
+
+    def getLoadBalancingCosts(self):
+        """dryRun cost of every volume node in common order, summed over the
+        mirrors and divided by the number of unique surface points
+        (kd_tree.F90:789-830, initializeWarping.F90:258-266)."""
+        costs = np.zeros(self.nVol)
+        self._chk(self.lib.idw_dry_run_costs(self.ctx, C.c_void_p(costs.ctypes.data), self.nVol, _lib.IDW_HOST), "dryRun")
+        return costs
 
     def setSurfaceDefinitionFromFile(self, surfFile):
         """Surface definition from a multiblock PLOT3D surface file (quads)."""

@@ -23,10 +23,11 @@ IDW_ERR_CUDA = -3
 IDW_ERR_NONFINITE = -4
 IDW_ERR_LIMIT = -5
 IDW_ERR_NOMEM = -6
+IDW_ERR_RESTART = -7
 
 _ERRNAMES = {
     -1: "IDW_ERR_ARG", -2: "IDW_ERR_STATE", -3: "IDW_ERR_CUDA", -4: "IDW_ERR_NONFINITE",
-    -5: "IDW_ERR_LIMIT", -6: "IDW_ERR_NOMEM",
+    -5: "IDW_ERR_LIMIT", -6: "IDW_ERR_NOMEM", -7: "IDW_ERR_RESTART",
 }
 
 
@@ -103,6 +104,9 @@ _SIGS = {
     "idw_warp_deriv_noalloc": [_VP, _VP, C.c_int64, _VP, C.c_int64],
     "idw_autotune": [_VP, C.c_int32, C.c_int32, C.POINTER(idw_tuning)],
     "idw_get_denominator0": [_VP, _VP, C.c_int64, C.c_int],
+    "idw_compute_denominator0": [_VP],
+    "idw_set_denominator0": [_VP, _VP, C.c_int64, C.c_int64, C.c_int],
+    "idw_dry_run_costs": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_denominator": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_stats": [_VP, C.POINTER(idw_stats)],
     "idw_get_tree": [_VP, _IP, _DP, _DP, _DP],

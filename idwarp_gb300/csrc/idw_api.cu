@@ -69,6 +69,7 @@ struct Ctx {
     DevBuf<int> parent;
     DevBuf<unsigned> nodeFlags;
     bool haveTree = false, haveWarp = false, nodalValid = false;
+    bool den0Valid = false;  // denominator estimate and walk records (computed at the first walk, or loaded)
     // FP32 companion arrays of the mixed-precision walk
     DevBuf<NodeRecF> nodeRec;
     DevBuf<float4> ptDA, ptDL;
@@ -242,6 +243,27 @@ int refresh_nodal(Ctx *c) {
     return check_launch(c, "nodal properties");
 }
 
+// Walk records of every volume node from the denominator estimate in den0.
+int finish_den0(Ctx *c) {
+    launch_walk_records(vol_dev(c), c->sym, c->optInit.bExp, c->recHi.p, c->recLo.p, c->stream);
+    int e = check_launch(c, "walk records");
+    if (e) return e;
+    c->gdenValid = false;
+    c->den0Valid = true;
+    return IDW_OK;
+}
+
+// The denominator estimate over the mirrors (initializeWarping.F90:241-247),
+// unless it was computed or loaded since the last initialize.
+int ensure_den0(Ctx *c) {
+    if (c->den0Valid) return IDW_OK;
+    CK(cudaSetDevice(c->device));
+    launch_denominator0(tree_dev(c), c->ptXA.p, vol_dev(c), make_init_law(c), c->sym, c->den0.p, c->stream);
+    int e = check_launch(c, "denominator0");
+    if (e) return e;
+    return finish_den0(c);
+}
+
 bool all_finite(const double *v, size_t n) {
     for (size_t i = 0; i < n; ++i)
         if (!std::isfinite(v[i])) return false;
@@ -383,6 +405,9 @@ int idw_create_common_grid(void *ctx, const double *volnodes, int64_t nvol, int 
         if (e) return e;
     }
     c->haveVolume = true;
+    // a new volume needs a new initialize (records and estimates are per node)
+    c->haveTree = false;
+    c->den0Valid = false;
     c->haveWarp = false;
     c->haveDxs = false;
     c->stats.nVol = nvol;
@@ -599,18 +624,14 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
         CK(cudaMemcpyAsync(c->ptDL.p, dl.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));
     }
-    // denominator estimate over the mirrors (initializeWarping.F90:241-247)
-    launch_denominator0(tree_dev(c), c->ptXA.p, vol_dev(c), law0, c->sym, c->den0.p, st);
-    e = check_launch(c, "denominator0");
-    if (e) return e;
+    // the denominator estimate and the walk records follow at the first walk
+    // (ensure_den0), or come from idw_compute_denominator0 / idw_set_denominator0
     CKA(c->recHi.alloc(size_t(c->sym.nLoop) * c->nVol));
     CKA(c->recLo.alloc(size_t(c->sym.nLoop) * c->nVol));
     CKA(c->acc.alloc(2 * size_t(c->nVol)));
     CKA(c->gden.alloc(size_t(c->nVol)));
     c->gdenValid = false;
-    launch_walk_records(vol_dev(c), c->sym, c->optInit.bExp, c->recHi.p, c->recLo.p, st);
-    e = check_launch(c, "walk records");
-    if (e) return e;
+    c->den0Valid = false;
     CK(cudaStreamSynchronize(st));
     c->haveTree = true;
     c->stats.nUnique = n;
@@ -681,6 +702,7 @@ static int ensure_gate_den(Ctx *c, const TreeDevF &tf, const PointsDevF &pf, con
 
 static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     int rc = refresh_nodal(c);
     if (rc) return rc;
     EvalConsts k;
@@ -848,6 +870,7 @@ int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double 
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     if (nbatch < 0 || !coords || !out) return fail(c, IDW_ERR_ARG, "bad batch arguments");
     CK(cudaSetDevice(c->device));
     const size_t sdof = 3 * size_t(c->nPts), vdof = 3 * size_t(c->nVol);
@@ -940,9 +963,77 @@ int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where) {
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     if (nvol != c->nVol) return fail(c, IDW_ERR_ARG, "nvol mismatch");
     CK(cudaSetDevice(c->device));
     return copy_out(c, out, c->den0.p, size_t(nvol), where);
+}
+
+int idw_compute_denominator0(void *ctx) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_set_denominator0(void *ctx, const double *den0, int64_t nvol, int64_t checkStride, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (nvol != c->nVol) return fail(c, IDW_ERR_ARG, "nvol mismatch: expected %lld, received %lld",
+                                     (long long)c->nVol, (long long)nvol);
+    if (nvol > 0 && !den0) return fail(c, IDW_ERR_ARG, "null denominator pointer");
+    if (where != IDW_DEVICE && !all_finite(den0, size_t(nvol)))
+        return fail(c, IDW_ERR_NONFINITE, "non-finite denominator estimate");
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    DevBuf<double> tmp;
+    CKA(tmp.alloc(size_t(nvol)));
+    int rc = copy_in(c, tmp.p, den0, size_t(nvol), where);
+    if (rc) return rc;
+    if (checkStride > 0 && nvol > 0) {
+        // initializeWarping.F90:190-209: re-estimate every checkStride-th node
+        const int64_t m = (nvol + checkStride - 1) / checkStride;
+        DevBuf<double> est;
+        CKA(est.alloc(size_t(m)));
+        launch_denominator0_strided(tree_dev(c), c->ptXA.p, vol_dev(c), make_init_law(c), c->sym, checkStride,
+                                    est.p, st);
+        rc = check_launch(c, "denominator0 check");
+        if (rc) return rc;
+        std::vector<double> e(m), l(m);
+        CK(cudaMemcpyAsync(e.data(), est.p, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpy2DAsync(l.data(), sizeof(double), tmp.p, sizeof(double) * size_t(checkStride), sizeof(double),
+                             size_t(m), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int64_t k = 0; k < m; ++k)
+            if (1.0 - e[k] / l[k] > 1e-15)
+                return fail(c, IDW_ERR_RESTART, "denominator0 of node %lld: loaded %.17g, estimate %.17g",
+                            (long long)(k * checkStride), l[k], e[k]);
+    }
+    CK(cudaMemcpyAsync(c->den0.p, tmp.p, sizeof(double) * size_t(nvol), cudaMemcpyDeviceToDevice, st));
+    c->haveWarp = c->haveDxs = false;
+    rc = finish_den0(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(st));
+    return IDW_OK;
+}
+
+int idw_dry_run_costs(void *ctx, double *costs, int64_t nvol, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
+    if (nvol != c->nVol) return fail(c, IDW_ERR_ARG, "nvol mismatch");
+    CK(cudaSetDevice(c->device));
+    DevBuf<double> out;
+    CKA(out.alloc(size_t(nvol)));
+    if (nvol > 0) CK(cudaMemsetAsync(out.p, 0, sizeof(double) * size_t(nvol), c->stream));
+    launch_dry_run(tree_dev(c), vol_dev(c), c->sym, c->opt.errTol, c->nUnique, out.p, c->stream);
+    int rc = check_launch(c, "dryRun costs");
+    if (rc) return rc;
+    return copy_out(c, costs, out.p, size_t(nvol), where);
 }
 
 int idw_get_denominator(void *ctx, double *out, int64_t nvol, int where) {
@@ -957,6 +1048,7 @@ int idw_get_denominator(void *ctx, double *out, int64_t nvol, int where) {
 static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStride, double *dxsOut, int where,
                      int64_t dxsStride) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDeriv");
     int rc = refresh_nodal(c);
     if (rc) return rc;
@@ -1211,6 +1303,7 @@ int idw_warp_deriv_fwd(void *ctx, const double *dxs, int64_t cdof, double *dxv, 
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDerivFwd");
     if (!dxs || !dxv) return fail(c, IDW_ERR_ARG, "null dXs or dXv");
     if (cdof != 3 * int64_t(c->nPts))
@@ -1382,6 +1475,7 @@ int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *d
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDeriv");
     if (!dxv || !dxs) return fail(c, IDW_ERR_ARG, "null dXv or dXs");
     if (ndof != 3 * c->nVol)
@@ -1557,6 +1651,7 @@ int idw_warp_deriv_fwd_batch(void *ctx, const double *dxs, int32_t ndir, double 
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (int e0 = ensure_den0(c)) return e0;
     if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDerivFwd");
     if (ndir < 0 || !dxs || !dxv) return fail(c, IDW_ERR_ARG, "bad tangent arguments");
     CK(cudaSetDevice(c->device));

@@ -135,6 +135,11 @@ void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &
                            double *scratch, int64_t scratchLen, cudaStream_t st);
 void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
                          const SymPlanes &sym, double *den0, cudaStream_t st);
+// estimate of the common-order nodes 0, stride, 2 stride, ... into out; returns their count
+int64_t launch_denominator0_strided(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
+                                    const SymPlanes &sym, int64_t stride, double *out, cudaStream_t st);
+void launch_dry_run(const TreeDev &t, const VolumeDev &v, const SymPlanes &sym, double errTol, int nPts,
+                    double *costs, cudaStream_t st);
 void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,
                          unsigned long long *codes, int *idx, cudaStream_t st);
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,

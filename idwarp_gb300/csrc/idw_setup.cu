@@ -2,6 +2,8 @@
 // volume nodes and the FP32 companion arrays of the mixed-precision path.
 //   computeErrors  src/modules/kd_tree.F90:832-880 (+ getSpherePts, src/utils/getSpherePts.F90)
 //   getWiEstimate  src/modules/kd_tree.F90:751-787, driven by src/warp/initializeWarping.F90:241-247
+//   restart check  src/warp/initializeWarping.F90:190-209 (every stride-th node re-estimated)
+//   dryRun         src/modules/kd_tree.F90:789-830, driven by src/warp/initializeWarping.F90:258-266
 #include <cub/cub.cuh>
 
 #include <vector>
@@ -115,10 +117,13 @@ __global__ void k_err_final(TreeDev t, WeightLaw law, const int *nodeItem0, cons
 
 // Denominator estimate: warp-cooperative walk with the 5-radius far-field
 // rule; every lane follows exactly its own recursion of getWiEstimate.
-__global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, SymPlanes sym, double *den0) {
+// stride 0: every node in Morton order, out[common index]; stride > 0: the
+// common-order nodes 0, stride, 2 stride, ... (nOut of them), out[k].
+__global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, SymPlanes sym, int64_t stride,
+                       int64_t nOut, double *out) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const bool valid = gid < v.nVol;
-    const int vi = valid ? v.perm[gid] : 0;
+    const bool valid = gid < nOut;
+    const int vi = !valid ? 0 : (stride > 0 ? int(gid * stride) : v.perm[gid]);
     double x0[3] = {v.xv0[3 * vi], v.xv0[3 * vi + 1], v.xv0[3 * vi + 2]};
     double acc = 0.0;
     for (int kk = 0; kk < sym.nLoop; ++kk) {
@@ -155,7 +160,53 @@ __global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, 
             }
         }
     }
-    if (valid) den0[vi] = acc;
+    if (valid) out[stride > 0 ? gid : int64_t(vi)] = acc;
+}
+
+// Load-balancing cost of every volume node: per mirror, leaves cost their
+// point count, every interior visit 0.5 and an accepted approximation 1.1
+// more; the sum over mirrors of cost / nPts.  Decisions as dryRun takes them:
+// dist with the 1e-16 softening and errTol * den0 as the tolerance.
+__global__ void k_dry_run(TreeDev t, VolumeDev v, SymPlanes sym, double errTol, double nPts, double *costs) {
+    const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool valid = gid < v.nVol;
+    const int vi = valid ? v.perm[gid] : 0;
+    const double x0[3] = {v.xv0[3 * vi], v.xv0[3 * vi + 1], v.xv0[3 * vi + 2]};
+    const double tolDen = errTol * v.den0[vi];
+    double acc = 0.0;
+    for (int kk = 0; kk < sym.nLoop; ++kk) {
+        double r[3];
+        mirror_point(sym, kk, x0, r);
+        double cst = 0.0;
+        int node = 0, skip = 0;
+        while (node < t.nNodes) {
+            const int4 inf = t.info[node];
+            const bool active = valid && node >= skip;
+            if (inf.w) {
+                if (active) cst += double(inf.y - inf.x + 1);
+                node = inf.z;
+            } else {
+                bool open = false;
+                if (active) {
+                    const dbl4 g = t.geom[node];
+                    const double r0 = r[0] - g.x, r1 = r[1] - g.y, r2 = r[2] - g.z;
+                    const double dist = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + 1e-16);
+                    cst += 0.5;
+                    if (dist * g.w < 2.0) {
+                        open = true;
+                    } else if (get_error64(t.err + kNerr * node, dist * g.w) < tolDen) {
+                        cst += 1.1;
+                        skip = inf.z;
+                    } else {
+                        open = true;
+                    }
+                }
+                node = __any_sync(kFull, open) ? node + 1 : inf.z;
+            }
+        }
+        acc += cst / nPts;
+    }
+    if (valid) costs[vi] = acc;
 }
 
 __device__ __forceinline__ unsigned long long spread21(unsigned long long x) {
@@ -327,7 +378,19 @@ void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &
 
 void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
                          const SymPlanes &sym, double *den0, cudaStream_t st) {
-    if (v.nVol > 0) k_den0<<<blocks(v.nVol, 128), 128, 0, st>>>(t, ptXA, v, law, sym, den0);
+    if (v.nVol > 0) k_den0<<<blocks(v.nVol, 128), 128, 0, st>>>(t, ptXA, v, law, sym, 0, v.nVol, den0);
+}
+
+int64_t launch_denominator0_strided(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
+                                    const SymPlanes &sym, int64_t stride, double *out, cudaStream_t st) {
+    const int64_t n = stride > 0 ? (v.nVol + stride - 1) / stride : 0;
+    if (n > 0) k_den0<<<blocks(n, 128), 128, 0, st>>>(t, ptXA, v, law, sym, stride, n, out);
+    return n;
+}
+
+void launch_dry_run(const TreeDev &t, const VolumeDev &v, const SymPlanes &sym, double errTol, int nPts,
+                    double *costs, cudaStream_t st) {
+    if (v.nVol > 0 && nPts > 0) k_dry_run<<<blocks(v.nVol, 128), 128, 0, st>>>(t, v, sym, errTol, double(nPts), costs);
 }
 
 void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,

@@ -38,6 +38,7 @@ extern "C" {
 #define IDW_ERR_NONFINITE -4 /* non-finite coordinates detected */
 #define IDW_ERR_LIMIT -5     /* a fixed limit was exceeded (face size, symmetry planes) */
 #define IDW_ERR_NOMEM -6     /* device allocation failed */
+#define IDW_ERR_RESTART -7   /* a loaded denominator estimate failed its check (idw_set_denominator0) */
 
 #define IDW_HOST 0
 #define IDW_DEVICE 1
@@ -214,6 +215,29 @@ int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *d
 /* Denominator estimate denominator0 (nvol), in common order.
  * (initializeWarping.F90:241-247) */
 int idw_get_denominator0(void *ctx, double *out, int64_t nvol, int where);
+
+/* The denominator estimate is computed at the first walk after
+ * idw_initialize_warping unless it was computed or loaded before.
+ * idw_compute_denominator0 computes it now (the reference does so during
+ * initializewarping, initializeWarping.F90:241-247).  */
+int idw_compute_denominator0(void *ctx);
+
+/* Load denominator0 (nvol, common order) in place of computing it: the
+ * restart-file path of initializeWarping.F90:124-228.  The common-order nodes
+ * 0, checkStride, 2 checkStride, ... (the reference checks every 100th) are
+ * re-estimated first; if any has 1 - estimate/loaded > 1e-15 the load is
+ * refused with IDW_ERR_RESTART and the context is left as it was, otherwise
+ * the loaded values replace the estimate and a previous warp is forgotten
+ * (warpMesh must run again before warpDeriv).  checkStride <= 0 skips the
+ * check.  Non-finite values are refused (IDW_ERR_NONFINITE) when where is
+ * IDW_HOST. */
+int idw_set_denominator0(void *ctx, const double *den0, int64_t nvol, int64_t checkStride, int where);
+
+/* Load-balancing cost of every volume node (nvol, common order): dryRun
+ * (kd_tree.F90:789-830) summed over the mirrors and divided by the number of
+ * unique surface points, as initializeWarping.F90:258-266 accumulates it and
+ * the restart file stores it.  Uses the denominator estimate in force. */
+int idw_dry_run_costs(void *ctx, double *costs, int64_t nvol, int where);
 
 /* Denominator sum(w) of the last idw_warp_mesh (nvol), in common order; the
  * reference's module variable `denominator` (src/warp/warpMesh.F90:59-70),
