@@ -20,23 +20,37 @@ namespace idw {
 
 namespace {
 
-constexpr int kChunk = 8;  // leaf points reduced per shared-memory pass
-
+// Leaf points reduced per shared-memory pass: ten for the small-S forms (a
+// 9-point leaf of the default bucket in one pass), eight for the blocked one.
 template <int S>
 struct AdjSmem {
+    static constexpr int kChunk = S <= 4 ? 10 : 8;
     float nb[32][3 * S];       // seeds of every lane (numerator adjoints, scaled)
     float4 vb[kChunk][32];     // per point: w, w (r - C)
 };
 
-// Warp reduction of m point contributions (vb[0..m)) against the lanes'
-// seeds, accumulated into dst(p) + 12 * ... (P row-major then B).
+// Lands the four moment sums of term `target`, seed component c (seed s, axis
+// a): w -> B (slot 9 + a), w (r - C) -> row a of P (slots 3a .. 3a + 2).
+__device__ __forceinline__ void land_moments(double *adj, int64_t seedStride, int c, int64_t target, float w,
+                                             float m0, float m1, float m2) {
+    if (w == 0.f && m0 == 0.f && m1 == 0.f && m2 == 0.f) return;
+    const int s = c / 3, a = c - 3 * s;
+    double *d = adj + s * seedStride + 12 * target;
+    atomicAdd(d + 9 + a, double(w));
+    atomicAdd(d + 3 * a + 0, double(m0));
+    atomicAdd(d + 3 * a + 1, double(m1));
+    atomicAdd(d + 3 * a + 2, double(m2));
+}
+
+// Warp reduction of m point contributions (vb[0..m), terms base .. base+m-1)
+// against the lanes' seeds, blocked for many seeds: lane c owns seed
+// component c and all m terms.
 template <int S>
-__device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *targets, double *adj,
-                                             int64_t seedStride) {
+__device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
+    constexpr int kChunk = AdjSmem<S>::kChunk;
     const int lane = threadIdx.x & 31;
     __syncwarp();
     for (int c = lane; c < 3 * S; c += 32) {
-        const int s = c / 3, a = c - 3 * s;
         float acc[kChunk][4];
 #pragma unroll
         for (int p = 0; p < kChunk; ++p) acc[p][0] = acc[p][1] = acc[p][2] = acc[p][3] = 0.f;
@@ -54,17 +68,73 @@ __device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *t
             }
         }
 #pragma unroll
-        for (int p = 0; p < kChunk; ++p) {
-            if (p < m && acc[p][0] != 0.f) {
-                double *d = adj + s * seedStride + 12 * int64_t(targets[p]);
-                atomicAdd(d + 9 + a, double(acc[p][0]));
-                atomicAdd(d + 3 * a + 0, double(acc[p][1]));
-                atomicAdd(d + 3 * a + 1, double(acc[p][2]));
-                atomicAdd(d + 3 * a + 2, double(acc[p][3]));
-            }
-        }
+        for (int p = 0; p < kChunk; ++p)
+            if (p < m) land_moments(adj, seedStride, c, base + p, acc[p][0], acc[p][1], acc[p][2], acc[p][3]);
     }
     __syncwarp();
+}
+
+// The same reduction for few seeds: one (term, seed component) pair per lane
+// task, so that 3 S m tasks keep the warp busy where 3 S lanes alone would
+// not.  Each task walks the lanes starting at its term index, which spreads
+// the tasks of different terms over the shared-memory banks.
+template <int S>
+__device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    for (int task = lane; task < 3 * S * m; task += 32) {
+        const int p = task / (3 * S), c = task - p * (3 * S);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll 8
+        for (int l0 = 0; l0 < 32; ++l0) {
+            const int l = (l0 + p) & 31;
+            const float nbv = sm.nb[l][c];
+            const float4 v = sm.vb[p][l];
+            a0 = fmaf(v.x, nbv, a0);
+            a1 = fmaf(v.y, nbv, a1);
+            a2 = fmaf(v.z, nbv, a2);
+            a3 = fmaf(v.w, nbv, a3);
+        }
+        land_moments(adj, seedStride, c, base + p, a0, a1, a2, a3);
+    }
+    __syncwarp();
+}
+
+// One seed, one term: the 12 products v (x) n of every lane summed over the
+// warp with shuffles.  Two halving exchanges (xor 16, 8) leave lane group
+// G = lane >> 3 with the 3 products of moment G; three butterflies (xor 4, 2,
+// 1) complete the sums; lanes 0..2 of each group land them.  Called by all 32
+// lanes.
+__device__ __forceinline__ void reduce_one_s1(const float4 v, const float n[3], double *d) {
+    const int lane = threadIdx.x & 31;
+    const float vc[4] = {v.x, v.y, v.z, v.w};
+    float P[12];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) P[3 * k + a] = vc[k] * n[a];
+    const bool h16 = lane & 16, h8 = lane & 8;
+    float Q[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float send = h16 ? P[k] : P[k + 6];
+        Q[k] = (h16 ? P[k + 6] : P[k]) + __shfl_xor_sync(kFull, send, 16);
+    }
+    float R[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float send = h8 ? Q[k] : Q[k + 3];
+        R[k] = (h8 ? Q[k + 3] : Q[k]) + __shfl_xor_sync(kFull, send, 8);
+    }
+#pragma unroll
+    for (int o = 4; o; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) R[k] += __shfl_xor_sync(kFull, R[k], o);
+    const int G = lane >> 3, a = lane & 7;
+    if (a < 3) {
+        const float val = a == 0 ? R[0] : (a == 1 ? R[1] : R[2]);
+        if (val != 0.f) atomicAdd(d + (G == 0 ? 9 + a : 3 * a + G - 1), double(val));
+    }
 }
 
 template <int S, int KIND>
@@ -91,7 +161,8 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
     // numb = dXv / den with den in the scaled units of the walk's weights
     const double q = valid ? exp2(-double(s) * mp.bExp) / den[vi] : 0.0;
     MixedCounters cnt;
-    int targets[kChunk];
+    constexpr int kChunk = AdjSmem<S>::kChunk;
+    float nl[3] = {0.f, 0.f, 0.f};  // one seed: this lane's, kept in registers
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
         const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
@@ -113,6 +184,11 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
             sm.nb[lane][3 * sd] = n3[0];
             sm.nb[lane][3 * sd + 1] = n3[1];
             sm.nb[lane][3 * sd + 2] = n3[2];
+            if (S == 1) {
+                nl[0] = n3[0];
+                nl[1] = n3[1];
+                nl[2] = n3[2];
+            }
         }
         __syncwarp();
         int node = 0, skip = 0;
@@ -138,7 +214,6 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         const int m = min(kChunk, inf.y - i0 + 1);
                         for (int p = 0; p < m; ++p) {
                             const int i = i0 + p;
-                            targets[p] = i;
                             float w = 0.f;
                             if (active) {
                                 const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
@@ -151,7 +226,10 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                             }
                             sm.vb[p][lane] = make_float4(w, w * R0, w * R1, w * R2);
                         }
-                        reduce_terms<S>(sm, m, targets, ptAdj, ptStride);
+                        if constexpr (S <= 4)
+                            reduce_tasks<S>(sm, m, i0, ptAdj, ptStride);
+                        else
+                            reduce_terms<S>(sm, m, i0, ptAdj, ptStride);
                     }
                 }
                 node = inf.z;
@@ -171,9 +249,16 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         skip = inf.z;
                         cnt.approx++;
                     }
-                    targets[0] = node;
-                    sm.vb[0][lane] = make_float4(w, w * rho0, w * rho1, w * rho2);
-                    reduce_terms<S>(sm, 1, targets, nodeAdj, nodeStride);
+                    const float4 vv = make_float4(w, w * rho0, w * rho1, w * rho2);
+                    if constexpr (S == 1) {
+                        reduce_one_s1(vv, nl, nodeAdj + 12 * int64_t(node));
+                    } else {
+                        sm.vb[0][lane] = vv;
+                        if constexpr (S <= 4)
+                            reduce_tasks<S>(sm, 1, node, nodeAdj, nodeStride);
+                        else
+                            reduce_terms<S>(sm, 1, node, nodeAdj, nodeStride);
+                    }
                 }
                 if (dec != 1 && active) open = true;
                 node = __any_sync(kFull, open) ? node + 1 : inf.z;
