@@ -395,6 +395,8 @@ def main():
     ap.add_argument("--config", default="P", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--mode", default="fast", choices=["fast", "exact"],
+                    help="evalMode of the timed warp; the extra measurements and the CPU baseline are fast-mode only")
     ap.add_argument("--suite", action="store_true", help="measurement table rows (S1, W, P errTol sweep)")
     ap.add_argument("--suite-d", action="store_true", help="the 20M-node two-body FFD loop")
     args = ap.parse_args()
@@ -407,7 +409,7 @@ def main():
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
     local_rank = _env_int("LOCAL_RANK", 0)
-    metric = "volume nodes warped/s (mixed-precision fast warpMesh)"
+    metric = "volume nodes warped/s (mixed-precision %s warpMesh)" % args.mode
     unit = "volume nodes/s"
 
     if args.impl == "reference":
@@ -452,7 +454,7 @@ def main():
     m = make_workload(args.config)
     nvol, npts = len(m["xv0"]), len(m["pts"])
     t_setup = time.perf_counter()
-    mesh = build_mesh(m, "mixed")
+    mesh = build_mesh(m, "mixed", args.mode)
     setup_s = time.perf_counter() - t_setup
     L = mesh.lib
     stream = torch.cuda.current_stream()
@@ -510,7 +512,7 @@ def main():
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": "wing_shell_%dx%dx%d" % CONFIGS[args.config], "volume_nodes": nvol,
                    "surface_points": npts, "unique_surface_nodes": st["nUnique"], "errTol": ERR_TOL,
-                   "mode": "fast", "symmetry_planes": 1, "parallelism": "replicas" if world > 1 else "single",
+                   "mode": args.mode, "symmetry_planes": 1, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (Xv0+Xv+den0+den ~%.0f MB per step)" % (nvol * 64 / 1e6)},
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": int(xs_host.nbytes),
                 "d2h_bytes_per_step": int(grid.nbytes)},
@@ -529,7 +531,8 @@ def main():
     # nodes, profiles/k_walk_mixed_wing2M_full.md), scaled by volume nodes: the
     # traffic is the per-node records and accumulators, the tree stays in L2
     traffic = 94.0 * nvol
-    out["roofline"] = {"bound": "fp32", "kernel": "k_walk_mixed", "achieved": achieved, "unit": "TFLOP/s",
+    walk_kernel = "k_exact_mixed" if args.mode == "exact" else "k_walk_mixed"
+    out["roofline"] = {"bound": "fp32", "kernel": walk_kernel, "achieved": achieved, "unit": "TFLOP/s",
                        "peak": peak, "peak_source": "measured FFMA probe (idw_probe_ffma) in this run",
                        "frac": (achieved / peak) if (achieved and peak) else None,
                        "flops_per_launch": flops, "kernel_ms": kernel_ms, "traffic": traffic,
@@ -537,6 +540,8 @@ def main():
                        "hbm": {"achieved_GBs": traffic / (kernel_ms * 1e-3) / 1e9 if kernel_ms > 0 else None,
                                "peak_GBs": _measured_peak("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"}}
 
+    if args.mode == "exact":
+        args.no_extras = args.no_cpu_baseline = True
     if not args.no_extras:
         # FP64 plain GPU form on the same workload, and the precision of the mixed form against it
         xm = grid.reshape(-1, 3).copy()

@@ -101,6 +101,7 @@ class USMesh(BaseSolver):
             "precision": [str, ["mixed", "fp64"]],
             "mixedGate": [float, 2e-3],
             "diagnostics": [int, 0],
+            "exactSchedule": [str, ["auto", "tiled", "walk"]],
         }
 
     # ------------------------------------------------------------------
@@ -543,6 +544,7 @@ class USMesh(BaseSolver):
         o.precision = _lib.IDW_PREC_MIXED if self.getOption("precision") == "mixed" else _lib.IDW_PREC_FP64
         o.mixedGate = self.getOption("mixedGate")
         o.diagnostics = self.getOption("diagnostics")
+        o.exactSchedule = {"auto": 0, "tiled": 1, "walk": 2}[self.getOption("exactSchedule")]
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

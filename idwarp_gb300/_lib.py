@@ -37,7 +37,7 @@ class idw_options(C.Structure):
         ("errTol", C.c_double), ("symmTol", C.c_double), ("cornerAngle", C.c_double),
         ("evalMode", C.c_int32), ("useRotations", C.c_int32), ("zeroCornerRotations", C.c_int32),
         ("bucketSize", C.c_int32), ("precision", C.c_int32), ("diagnostics", C.c_int32),
-        ("mixedGate", C.c_double), ("reserved", C.c_int32 * 4),
+        ("mixedGate", C.c_double), ("exactSchedule", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 

@@ -72,6 +72,8 @@ struct Ctx {
     bool den0Valid = false;  // denominator estimate and walk records (computed at the first walk, or loaded)
     // FP32 companion arrays of the mixed-precision walk
     DevBuf<NodeRecF> nodeRec;
+    DevBuf<int4> leafList;  // leaves in preorder (exact-mode kernel)
+    int nLeaves = 0;
     DevBuf<float4> ptDA, ptDL;
     DevBuf<float4> recHi, recLo, acc;  // per-volume-node walk records and accumulators
     DevBuf<float> gden;                // per node: scaled denominator of a mixed walk (precision gate)
@@ -205,6 +207,15 @@ SurfaceDev surf_dev(Ctx *c) {
     return s;
 }
 
+TreeDevF tree_devf(Ctx *c) {
+    TreeDevF tf;
+    tf.nodes = c->nodeRec.p;
+    tf.leaves = c->leafList.p;
+    tf.nLeaves = c->nLeaves;
+    tf.nPts = c->nUnique;
+    return tf;
+}
+
 VolumeDev vol_dev(Ctx *c) {
     VolumeDev v;
     v.nVol = c->nVol;
@@ -223,6 +234,8 @@ int validate_options(Ctx *c, const idw_options *o) {
     if (o->bucketSize < 1) return fail(c, IDW_ERR_ARG, "bucketSize must be >= 1");
     if (!(o->LdefFact > 0.0)) return fail(c, IDW_ERR_ARG, "LdefFact must be > 0");
     if (!(o->mixedGate >= 0.0)) return fail(c, IDW_ERR_ARG, "mixedGate must be >= 0");
+    if (o->exactSchedule < IDW_EXACT_AUTO || o->exactSchedule > IDW_EXACT_WALK)
+        return fail(c, IDW_ERR_ARG, "exactSchedule must be IDW_EXACT_AUTO, IDW_EXACT_TILED or IDW_EXACT_WALK");
     return IDW_OK;
 }
 
@@ -555,6 +568,13 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     }
     CK(cudaMemcpyAsync(c->info.p, info.data(), sizeof(int4) * nn, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->geom.p, geom.data(), sizeof(dbl4) * nn, cudaMemcpyHostToDevice, st));
+    std::vector<int4> leaves;
+    for (int k = 0; k < nn; ++k)
+        if (t.leaf[k]) leaves.push_back(make_int4(t.l[k], t.u[k], k, 0));
+    c->nLeaves = int(leaves.size());
+    CKA(c->leafList.alloc(leaves.size()));
+    if (!leaves.empty())
+        CK(cudaMemcpyAsync(c->leafList.p, leaves.data(), sizeof(int4) * leaves.size(), cudaMemcpyHostToDevice, st));
     launch_tree_parents(tree_dev(c), c->parent.p, st);
     // initial nodal properties: normals0, Ai, corners (kd_tree.F90:1547-1578)
     SurfaceDev s = surf_dev(c);
@@ -710,6 +730,7 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = c->opt.diagnostics & 1;
+    k.exactSchedule = c->opt.exactSchedule;
     // terms whose weight x (motion + lever arm) exceeds mixedGate*Ldef*den0 are summed in double-float
     k.precGate = mixed_gate(c);
     PointsDev p;
@@ -723,8 +744,7 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     CK(cudaEventRecord(c->ev0, c->stream));
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     if (c->opt.precision == IDW_PREC_MIXED) {
-        TreeDevF tf;
-        tf.nodes = c->nodeRec.p;
+        const TreeDevF tf = tree_devf(c);
         PointsDevF pf;
         pf.da = c->ptDA.p;
         pf.dl = c->ptDL.p;
@@ -833,10 +853,10 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = 0;
+    k.exactSchedule = c->opt.exactSchedule;
     k.precGate = tangent ? tangentGate : mixed_gate(c);
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
-    TreeDevF tf;
-    tf.nodes = c->nodeRec.p;
+    const TreeDevF tf = tree_devf(c);
     PointsDevF pf;
     pf.da = c->ptDA.p;
     pf.dl = c->ptDL.p;
@@ -1057,6 +1077,7 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = 0;
+    k.exactSchedule = c->opt.exactSchedule;
     k.precGate = 0.0;
     PointsDev p;
     p.xa = c->ptXA.p;
@@ -1079,8 +1100,7 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     CK(cudaEventRecord(c->ev0, c->stream));
     if (mixed) {
-        TreeDevF tf;
-        tf.nodes = c->nodeRec.p;
+        const TreeDevF tf = tree_devf(c);
         PointsDevF pf;
         pf.da = c->ptDA.p;
         pf.dl = c->ptDL.p;
@@ -1239,6 +1259,7 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = 0;
+    k.exactSchedule = c->opt.exactSchedule;
     k.precGate = 0.0;
     WalkOut o;
     o.xv = xvdDev;
@@ -1263,8 +1284,7 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
         launch_mixed_nodes(tree_dev(c), nodeMBd.p, ptMBd.p, c->nodeDC.p, c->nodeDCl.p, c->nodeDn.p, c->refDB.p,
                            c->stream);
         c->nodalValid = false;
-        TreeDevF tf;
-        tf.nodes = c->nodeRec.p;
+        const TreeDevF tf = tree_devf(c);
         PointsDevF pf;
         pf.da = c->ptDA.p;
         pf.dl = c->ptDL.p;
@@ -1503,6 +1523,7 @@ int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *d
     k.errTol = c->opt.errTol;
     k.sym = c->sym;
     k.slotStats = 0;
+    k.exactSchedule = c->opt.exactSchedule;
     k.precGate = 0.0;
     const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     // the accumulators start at zero
@@ -1510,8 +1531,7 @@ int idw_warp_deriv_noalloc(void *ctx, const double *dxv, int64_t ndof, double *d
     CK(cudaMemsetAsync(nodeAdj, 0, sizeof(double) * 12 * size_t(nn), c->stream));
     CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     if (mixed) {
-        TreeDevF tf;
-        tf.nodes = c->nodeRec.p;
+        const TreeDevF tf = tree_devf(c);
         PointsDevF pf;
         pf.da = c->ptDA.p;
         pf.dl = c->ptDL.p;

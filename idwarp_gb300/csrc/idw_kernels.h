@@ -45,6 +45,10 @@ struct __align__(128) NodeRecF {
 
 struct TreeDevF {
     const NodeRecF *nodes;
+    // leaves in preorder: (l, u, node, 0); their point ranges tile [0, n)
+    const int4 *leaves = nullptr;
+    int nLeaves = 0;
+    int nPts = 0;  // unique surface points (tree order)
 };
 
 // Surface point data for the evaluation kernels, tree order.
@@ -109,6 +113,7 @@ struct EvalConsts {
     SymPlanes sym;
     int slotStats;
     double precGate;  // mixed walk: weight x lever-arm threshold for double-float cluster terms
+    int exactSchedule = 0;  // IDW_EXACT_AUTO / _TILED / _WALK (mixed exact mode)
 };
 
 // Nodal properties (idw_nodal.cu)
@@ -155,6 +160,14 @@ void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, 
 void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
                        const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
                        const WalkOut &o, cudaStream_t st);
+// Exact mode as a tiled N-body kernel (idw_exact.cu); launch_walk_mixed uses
+// it for exact = 1.  Fills acc like the walk; no finalisation.
+void launch_exact_mixed(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, const VolumeDev &v,
+                        const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, float4 *acc,
+                        unsigned long long *counters, cudaStream_t st);
+// True when the tiled exact kernel has volume nodes for at least two full
+// waves of the device (below that the walk's finer grain is faster).
+bool exact_tiled_fills(int64_t nVol);
 // Per node (Morton order): the scaled denominator of the last mixed walk (acc).
 void launch_gate_den(int64_t nVol, const float4 *acc, float *gden, cudaStream_t st);
 int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,

@@ -18,6 +18,7 @@
 // with the FP64 decision of the FP64 form (decide64), so the mixed walk makes
 // exactly the FP64 walk's decisions.
 #include "idw_mixed.cuh"
+#include "idwarp_gb300.h"
 
 namespace idw {
 
@@ -35,29 +36,11 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = gid < v.nVol;
     const int64_t g = valid ? gid : 0;
-    // per-node scale sigma = 2^s (set-up constant, stored with the record)
-    const float4 r0lo = rec.lo[g];
-    const int s = __float_as_int(r0lo.w);
-    const float den0f = rec.hi[g].w;
-    const float Ls = mp.LdefF * pow2f(s);
-    const float LsLo = mp.LdefLo * pow2f(s);
-    const float c1 = mp.intExp ? pow2f(s * mp.dExp) : exp2f(float(s) * mp.dExpF);
+    // per-node scale sigma = 2^s (set-up constant, stored with the record),
+    // FP32 decision tolerance and precision gate
+    const NodeScale ns = node_scale(rec, mp, g);
+    const float Ls = ns.Ls, LsLo = ns.LsLo, c1 = ns.c1, tauf = ns.tauf, gv = ns.gv;
     const float ab = mp.abH, abl = mp.abL;
-    const float tauf = mp.errTolF * den0f;
-    // precision gate: a term whose FP32 rounding, w (|S'| + |D'| |r - X|) u,
-    // could exceed mixedGate * Ldef * u of the final denominator is summed in
-    // double-float.  The final (scaled) denominator is the walk's own from an
-    // earlier pass (it depends on Xu0 and the weight law only), else the
-    // estimate den0 sigma^b (which overestimates it on the wall, where den0's
-    // softening 1e-16 is below the walk's 1e-15).
-    float gv;
-    if (rec.gden) {
-        gv = mp.precGate * rec.gden[g];
-    } else {
-        const float gexp = float(s) * mp.bExpF;
-        const float gexpi = floorf(gexp);
-        gv = mp.precGate * ldexpf(den0f, int(gexpi)) * exp2f(gexp - gexpi);
-    }
     // running sums over the mirrors (sum = S + C per component), kept in shared
     // memory between mirror passes to free registers for the walk
     __shared__ float4 mirS[128], mirC[128];
@@ -89,62 +72,21 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                     l2 += rl[2] - cl.z;
                     float pn0 = 0.f, pn1 = 0.f, pn2 = 0.f, pd = 0.f;
                     for (int i = inf.x; i <= inf.y; ++i) {
-                        const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
                         const float4 *dm = reinterpret_cast<const float4 *>(pf.dm + 12 * i);
-                        const float4 m0 = ldgf4(dm), m1 = ldgf4(dm + 1), m2 = ldgf4(dm + 2);
-                        const float dx = (h0 - da.x) + (l0 - dl.x);
-                        const float dy = (h1 - da.y) + (l1 - dl.y);
-                        const float dz = (h2 - da.z) + (l2 - dl.z);
-                        const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
-                        const float r1 = rsqrtf(d2);
-                        const float tt = fmaf(Ls, r1, LsLo * r1);
-                        const float w = da.w * law.eval(tt, c1, ab, abl);
-                        // S = D dx + u ; D row-major in m0.xyzw m1.xyzw m2.x, u in m2.yzw
-                        const float S0 = fmaf(m0.x, dx, fmaf(m0.y, dy, fmaf(m0.z, dz, m2.y)));
-                        const float S1 = fmaf(m0.w, dx, fmaf(m1.x, dy, fmaf(m1.y, dz, m2.z)));
-                        const float S2 = fmaf(m1.z, dx, fmaf(m1.w, dy, fmaf(m2.x, dz, m2.w)));
-                        pn0 = fmaf(w, S0, pn0);
-                        pn1 = fmaf(w, S1, pn1);
-                        pn2 = fmaf(w, S2, pn2);
-                        pd += w;
+                        leaf_pair<KIND>(law, Ls, LsLo, c1, ab, abl, h0, h1, h2, l0, l1, l2, ldgf4(pf.da + i),
+                                        ldgf4(pf.dl + i), ldgf4(dm), ldgf4(dm + 1), ldgf4(dm + 2), pn0, pn1, pn2, pd);
                     }
                     // a leaf carrying a large weight at a long lever arm is
                     // re-summed in double-float (same gate as cluster terms)
-                    const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) +
-                                       pd * __ldg(af.dn + node) * (fabsf(h0) + fabsf(h1) + fabsf(h2));
-                    leafPrecise = KIND != 2 && lmag > gv;
-                    if (!leafPrecise) {
-                        kahan_add(sn[0], cn[0], pn0);
-                        kahan_add(sn[1], cn[1], pn1);
-                        kahan_add(sn[2], cn[2], pn2);
-                        kahan_add(sd, cd, pd);
-                    }
+                    leafPrecise = leaf_close<KIND>(pn0, pn1, pn2, pd, __ldg(af.dn + node), h0, h1, h2, gv, sn, cn, sd,
+                                                   cd);
                     cnt.leafPairs += inf.y - inf.x + 1;
                     cnt.visited++;
                 }
                 if (__any_sync(kFull, leafPrecise)) {
-                    if (leafPrecise) {
-                        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
-                        dfl q0, q1, q2;
-                        two_diff(rh[0], ch.x, q0.h, q0.l);
-                        two_diff(rh[1], ch.y, q1.h, q1.l);
-                        two_diff(rh[2], ch.z, q2.h, q2.l);
-                        q0.l += rl[0] - cl.x;
-                        q1.l += rl[1] - cl.y;
-                        q2.l += rl[2] - cl.z;
-                        for (int i = inf.x; i <= inf.y; ++i) {
-                            const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
-                            dfl x[3];
-                            two_diff(q0.h, da.x, x[0].h, x[0].l);
-                            two_diff(q1.h, da.y, x[1].h, x[1].l);
-                            two_diff(q2.h, da.z, x[2].h, x[2].l);
-                            x[0].l += q0.l - dl.x;
-                            x[1].l += q1.l - dl.y;
-                            x[2].l += q2.l - dl.z;
-                            precise_term<KIND>(x, 1e-15f, da.w, dl.w, pf.dm + 12 * i, pf.dml + 12 * i, law, Ls, LsLo,
-                                               c1, mp.abH, mp.abL, sn, cn, sd, cd);
-                        }
-                    }
+                    if (leafPrecise)
+                        precise_leaf<KIND>(tf, pf, node, inf.x, inf.y, rh, rl, law, Ls, LsLo, c1, mp.abH, mp.abL, sn,
+                                           cn, sd, cd);
                     warp_count(counters, 6, leafPrecise ? unsigned(inf.y - inf.x + 1) : 0u);
                 }
                 node = inf.z;
@@ -200,44 +142,10 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                 node = __any_sync(kFull, open) ? node + 1 : inf.z;
             }
         }
-        // add the reference motion back: num += den (Dref r + bref), with r
-        // this mirror's point, in double-float
-        const dfl den = df_norm(sd, cd);
-        dfl num[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            dfl sr = {__ldg(af.ref + 9 + a), __ldg(af.ref + 21 + a)};
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                sr = df_add(sr, df_mul({__ldg(af.ref + 3 * a + k), __ldg(af.ref + 12 + 3 * a + k)}, {rh[k], rl[k]}));
-            num[a] = df_add(df_norm(sn[a], cn[a]), df_mul(den, sr));
-        }
-        // reflect this mirror's numerator back (vector reflection) and
-        // accumulate, all in double-float so no digits are lost between mirrors
-        if (mp.nLoop == 1) {
-            mirS[threadIdx.x] = make_float4(num[0].h, num[1].h, num[2].h, den.h);
-            mirC[threadIdx.x] = make_float4(num[0].l, num[1].l, num[2].l, den.l);
-        } else {
-#pragma unroll
-            for (int j = 0; j < kMaxSym; ++j) {
-                if (j < mp.nSym && ((kk >> j) & 1)) {
-                    const dfl n0 = {mp.nrm[j][0], mp.nrmLo[j][0]}, n1 = {mp.nrm[j][1], mp.nrmLo[j][1]},
-                              n2 = {mp.nrm[j][2], mp.nrmLo[j][2]};
-                    dfl dp = df_add(df_add(df_mul(num[0], n0), df_mul(num[1], n1)), df_mul(num[2], n2));
-                    dp = {-2.0f * dp.h, -2.0f * dp.l};
-                    num[0] = df_add(num[0], df_mul(dp, n0));
-                    num[1] = df_add(num[1], df_mul(dp, n1));
-                    num[2] = df_add(num[2], df_mul(dp, n2));
-                }
-            }
-            float4 S4 = mirS[threadIdx.x], C4 = mirC[threadIdx.x];
-            kahan_add_df(S4.x, C4.x, num[0]);
-            kahan_add_df(S4.y, C4.y, num[1]);
-            kahan_add_df(S4.z, C4.z, num[2]);
-            kahan_add_df(S4.w, C4.w, den);
-            mirS[threadIdx.x] = S4;
-            mirC[threadIdx.x] = C4;
-        }
+        float4 S4 = mirS[threadIdx.x], C4 = mirC[threadIdx.x];
+        finish_mirror(af, mp, kk, rh, rl, sn, cn, sd, cd, S4, C4);
+        mirS[threadIdx.x] = S4;
+        mirC[threadIdx.x] = C4;
     }
     if (valid) {
         acc[2 * gid] = mirS[threadIdx.x];
@@ -352,7 +260,11 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
     if (v.nVol <= 0) return;
     const int g = blocks(v.nVol, 128);
     const MixedParams mp = make_mixed_params(k);
-    if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
+    if (exact && tf.nLeaves > 0 && !mp.slotStats && k.exactSchedule != IDW_EXACT_WALK &&
+        (k.exactSchedule == IDW_EXACT_TILED || exact_tiled_fills(v.nVol))) {
+        // every pair: the tiled kernel, with the walk's arithmetic
+        launch_exact_mixed(tf, pf, af, v, rec, mp, k.law, acc, o.counters, st);
+    } else if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         Law32<0> law{3, 5, 3.f, 5.f};
         k_walk_mixed<0><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
     } else if (k.law.isInt) {

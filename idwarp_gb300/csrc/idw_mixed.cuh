@@ -323,4 +323,157 @@ __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const Volume
 // Power of two 2^e as a float (|e| <= 126).
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + max(-126, min(127, e))) << 23); }
 
+// Per-volume-node constants of the mixed evaluation, from its walk record:
+// sigma = 2^s scales the weights (Ls = Ldef sigma split in two floats, c1 =
+// sigma^(b-a)), tauf = errTol den0 (FP32 decisions), and the precision gate
+// gv: a term whose FP32 rounding, w (|S'| + |D'| |r - X|) u, could exceed
+// mixedGate * Ldef * u of the final denominator is summed in double-float.
+// The final (scaled) denominator is the walk's own from an earlier pass (it
+// depends on Xu0 and the weight law only), else the estimate den0 sigma^b
+// (which overestimates it on the wall, where den0's softening 1e-16 is below
+// the walk's 1e-15).
+struct NodeScale {
+    float Ls, LsLo, c1, tauf, gv;
+    int s;
+};
+__device__ __forceinline__ NodeScale node_scale(const WalkRecF &rec, const MixedParams &mp, int64_t g) {
+    NodeScale n;
+    const float4 r0lo = rec.lo[g];
+    n.s = __float_as_int(r0lo.w);
+    const float den0f = rec.hi[g].w;
+    n.Ls = mp.LdefF * pow2f(n.s);
+    n.LsLo = mp.LdefLo * pow2f(n.s);
+    n.c1 = mp.intExp ? pow2f(n.s * mp.dExp) : exp2f(float(n.s) * mp.dExpF);
+    n.tauf = mp.errTolF * den0f;
+    if (rec.gden) {
+        n.gv = mp.precGate * rec.gden[g];
+    } else {
+        const float gexp = float(n.s) * mp.bExpF;
+        const float gexpi = floorf(gexp);
+        n.gv = mp.precGate * ldexpf(den0f, int(gexpi)) * exp2f(gexp - gexpi);
+    }
+    return n;
+}
+
+// 1/sqrt(x) for a normal x (here x >= 1e-15): the flush-to-zero form of the
+// approximate reciprocal square root gives the value rsqrtf gives, without
+// rsqrtf's handling of subnormal inputs.
+__device__ __forceinline__ float rsqrt_normal(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// One leaf pair in FP32 (evalNodeExact's term, kd_tree.F90:664-690): h + l
+// is r - C (leaf centroid), da + dl the point's offset from C and its area,
+// m0..m2 the point's D' (row-major, 9) and u' (3); accumulates w S and w.
+template <int KIND>
+__device__ __forceinline__ void leaf_pair(const Law32<KIND> &law, float Ls, float LsLo, float c1, float ab,
+                                          float abl, float h0, float h1, float h2, float l0, float l1, float l2,
+                                          const float4 da, const float4 dl, const float4 m0, const float4 m1,
+                                          const float4 m2, float &pn0, float &pn1, float &pn2, float &pd) {
+    const float dx = (h0 - da.x) + (l0 - dl.x);
+    const float dy = (h1 - da.y) + (l1 - dl.y);
+    const float dz = (h2 - da.z) + (l2 - dl.z);
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
+    const float r1 = rsqrt_normal(d2);
+    const float tt = fmaf(Ls, r1, LsLo * r1);
+    const float w = da.w * law.eval(tt, c1, ab, abl);
+    // S = D dx + u ; D row-major in m0.xyzw m1.xyzw m2.x, u in m2.yzw
+    const float S0 = fmaf(m0.x, dx, fmaf(m0.y, dy, fmaf(m0.z, dz, m2.y)));
+    const float S1 = fmaf(m0.w, dx, fmaf(m1.x, dy, fmaf(m1.y, dz, m2.z)));
+    const float S2 = fmaf(m1.z, dx, fmaf(m1.w, dy, fmaf(m2.x, dz, m2.w)));
+    pn0 = fmaf(w, S0, pn0);
+    pn1 = fmaf(w, S1, pn1);
+    pn2 = fmaf(w, S2, pn2);
+    pd += w;
+}
+
+// End of a leaf: its partial sums go into the compensated running sums,
+// unless the leaf carries a large weight at a long lever arm (the cluster
+// terms' gate, with dn the leaf's bound on |D'|); returns true for such a
+// leaf, which the caller re-sums in double-float (precise_leaf).
+template <int KIND>
+__device__ __forceinline__ bool leaf_close(float pn0, float pn1, float pn2, float pd, float dn, float h0, float h1,
+                                           float h2, float gv, float *sn, float *cn, float &sd, float &cd) {
+    const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + pd * dn * (fabsf(h0) + fabsf(h1) + fabsf(h2));
+    const bool precise = KIND != 2 && lmag > gv;
+    if (!precise) {
+        kahan_add(sn[0], cn[0], pn0);
+        kahan_add(sn[1], cn[1], pn1);
+        kahan_add(sn[2], cn[2], pn2);
+        kahan_add(sd, cd, pd);
+    }
+    return precise;
+}
+
+// A leaf's terms (points lo..hi) re-summed in double-float.
+template <int KIND>
+__device__ __forceinline__ void precise_leaf(const TreeDevF &tf, const PointsDevF &pf, int node, int lo, int hi,
+                                             const float *rh, const float *rl, const Law32<KIND> &law, float Ls,
+                                             float LsLo, float c1, float abH, float abL, float *sn, float *cn,
+                                             float &sd, float &cd) {
+    const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+    dfl q0, q1, q2;
+    two_diff(rh[0], ch.x, q0.h, q0.l);
+    two_diff(rh[1], ch.y, q1.h, q1.l);
+    two_diff(rh[2], ch.z, q2.h, q2.l);
+    q0.l += rl[0] - cl.x;
+    q1.l += rl[1] - cl.y;
+    q2.l += rl[2] - cl.z;
+    for (int i = lo; i <= hi; ++i) {
+        const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
+        dfl x[3];
+        two_diff(q0.h, da.x, x[0].h, x[0].l);
+        two_diff(q1.h, da.y, x[1].h, x[1].l);
+        two_diff(q2.h, da.z, x[2].h, x[2].l);
+        x[0].l += q0.l - dl.x;
+        x[1].l += q1.l - dl.y;
+        x[2].l += q2.l - dl.z;
+        precise_term<KIND>(x, 1e-15f, da.w, dl.w, pf.dm + 12 * i, pf.dml + 12 * i, law, Ls, LsLo, c1, abH, abL, sn,
+                           cn, sd, cd);
+    }
+}
+
+// End of one mirror pass: add the reference motion back, num += den (Dref r +
+// bref) with r the mirror's point, reflect the numerator back (vector
+// reflection) and add (num, den) into the running pair S4 + C4, all in
+// double-float so no digits are lost between mirrors.  S4, C4 are overwritten
+// when there is a single pass.
+__device__ __forceinline__ void finish_mirror(const NodeAggF &af, const MixedParams &mp, int kk, const float *rh,
+                                              const float *rl, const float *sn, const float *cn, float sd, float cd,
+                                              float4 &S4, float4 &C4) {
+    const dfl den = df_norm(sd, cd);
+    dfl num[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        dfl sr = {__ldg(af.ref + 9 + a), __ldg(af.ref + 21 + a)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            sr = df_add(sr, df_mul({__ldg(af.ref + 3 * a + k), __ldg(af.ref + 12 + 3 * a + k)}, {rh[k], rl[k]}));
+        num[a] = df_add(df_norm(sn[a], cn[a]), df_mul(den, sr));
+    }
+    if (mp.nLoop == 1) {
+        S4 = make_float4(num[0].h, num[1].h, num[2].h, den.h);
+        C4 = make_float4(num[0].l, num[1].l, num[2].l, den.l);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxSym; ++j) {
+        if (j < mp.nSym && ((kk >> j) & 1)) {
+            const dfl n0 = {mp.nrm[j][0], mp.nrmLo[j][0]}, n1 = {mp.nrm[j][1], mp.nrmLo[j][1]},
+                      n2 = {mp.nrm[j][2], mp.nrmLo[j][2]};
+            dfl dp = df_add(df_add(df_mul(num[0], n0), df_mul(num[1], n1)), df_mul(num[2], n2));
+            dp = {-2.0f * dp.h, -2.0f * dp.l};
+            num[0] = df_add(num[0], df_mul(dp, n0));
+            num[1] = df_add(num[1], df_mul(dp, n1));
+            num[2] = df_add(num[2], df_mul(dp, n2));
+        }
+    }
+    kahan_add_df(S4.x, C4.x, num[0]);
+    kahan_add_df(S4.y, C4.y, num[1]);
+    kahan_add_df(S4.z, C4.z, num[2]);
+    kahan_add_df(S4.w, C4.w, den);
+}
+
 }  // namespace idw

@@ -49,6 +49,10 @@ extern "C" {
 #define IDW_PREC_FP64 0  /* FP64 throughout (the plain form) */
 #define IDW_PREC_MIXED 1 /* FP32 distances/weights/accumulation, FP64 set-up and normalisation */
 
+#define IDW_EXACT_AUTO 0  /* exact-mode schedule chosen by mesh size */
+#define IDW_EXACT_TILED 1 /* shared-memory tiles of surface points, several volume nodes per thread */
+#define IDW_EXACT_WALK 2  /* the tree walk with every node opened */
+
 /* Mesh options: the gridinput module variables (src/modules/gridInput.f90:9-18,
  * libidwarp.pyf:148-162) plus kd_tree.bucket_size (libidwarp.pyf:204-206) and
  * the GB300 precision switch.  Semantics follow doc/options.yaml. */
@@ -71,7 +75,10 @@ typedef struct idw_options {
                            * plane) is summed in double-float (S' = the term's motion
                            * less the mean surface motion, den = the node's
                            * denominator; default 2e-3; 0 = every term) */
-    int32_t reserved[4];
+    int32_t exactSchedule; /* mixed exact mode: IDW_EXACT_AUTO (default: tiled
+                            * kernel when the mesh fills the GPU, else the walk),
+                            * IDW_EXACT_TILED or IDW_EXACT_WALK; same sums either way */
+    int32_t reserved[3];
 } idw_options;
 
 /* Work counters of the last warp / warpDeriv call. */
