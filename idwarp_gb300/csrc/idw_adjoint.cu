@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                                 const float dy = (h1 - da.y) + (l1 - dl.y);
                                 const float dz = (h2 - da.z) + (l2 - dl.z);
                                 const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
-                                const float r1 = rsqrtf(d2);
+                                const float r1 = rsqrt_normal(d2);
                                 w = da.w * law.eval(fmaf(Ls, r1, LsLo * r1), c1, ab, abl);
                             }
                             sm.vb[p][lane] = make_float4(w, w * R0, w * R1, w * R2);

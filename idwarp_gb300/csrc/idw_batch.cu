@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                         const float dy = (h1 - da.y) + (l1 - dl.y);
                         const float dz = (h2 - da.z) + (l2 - dl.z);
                         const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
-                        const float r1 = rsqrtf(d2);
+                        const float r1 = rsqrt_normal(d2);
                         const float tt = fmaf(Ls, r1, LsLo * r1);
                         const float w = da.w * law.eval(tt, c1, ab, abl);
 #pragma unroll
