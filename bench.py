@@ -607,7 +607,26 @@ def main():
                             "fp64_value": 16 * nvol / (msd64 * 1e-3), "fp64_ms": msd64,
                             "speedup_mixed_over_fp64": msd64 / msd,
                             "max_rel_diff_vs_fp64": float((dxs - dxs64).abs().max().item() / dref)}
-        del sd, dxs, dxs64
+
+        # one seed (the solver-adjoint call pattern): idw_warp_deriv on the device
+        def deriv1():
+            rc = L.idw_warp_deriv(mesh.ctx, C.c_void_p(sd.data_ptr()), 3 * nvol, _lib.IDW_DEVICE)
+            if rc != 0:
+                _lib.check(L, mesh.ctx, rc, "warpDeriv")
+
+        deriv1()
+        barrier()
+        e0.record(stream)
+        for _ in range(5):
+            deriv1()
+        e1.record(stream)
+        barrier()
+        ms1 = e0.elapsed_time(e1) / 5
+        d1 = torch.tensor(mesh.getdXs(), device="cuda")
+        out["warpDeriv1"] = {"seeds": 1, "value": nvol / (ms1 * 1e-3), "unit": "seeds*nodes/s", "ms": ms1,
+                             "max_rel_diff_vs_fp64": float((d1 - dxs64[0]).abs().max().item()
+                                                           / dxs64[0].abs().max().item())}
+        del sd, dxs, dxs64, d1
         # 8 independent surface perturbations (seeds 200-207) through the batched
         # walk (four surfaces share one tree walk) against one warpMesh each
         from idwarp_gb300 import synthetic as S
