@@ -60,6 +60,7 @@ struct Ctx {
     DevBuf<double> xs, xu, normals0, ptMB, tmpAi;
     DevBuf<dbl4> ptXA;
     DevBuf<int> xuInd, facePtr, faceConn, n2ePtr, n2e, isCorner;
+    DevBuf<double> faceScratch;  // per face: area, normal and their adjoints (nodal kernels)
     // tree
     int nNodes = 0, maxDepth = 0;
     double Ldef0 = 0.0;
@@ -204,6 +205,8 @@ SurfaceDev surf_dev(Ctx *c) {
     s.faceConn = c->faceConn.p;
     s.n2ePtr = c->n2ePtr.p;
     s.n2e = c->n2e.p;
+    s.nFaces = c->nFaces;
+    s.faceScratch = c->faceScratch.p;
     return s;
 }
 
@@ -530,6 +533,7 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->xuInd.alloc(n));
     CKA(c->isCorner.alloc(n));
     CKA(c->facePtr.alloc(nfaces + 1));
+    CKA(c->faceScratch.alloc(8 * size_t(std::max(nfaces, 1))));
     CKA(c->faceConn.alloc(std::max(nconn, 1)));
     CKA(c->n2ePtr.alloc(n + 1));
     CKA(c->n2e.alloc(std::max(nconn, 1)));

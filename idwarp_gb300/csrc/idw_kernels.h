@@ -14,6 +14,9 @@ struct SurfaceDev {
     const int *faceConn; // tree-order vertex ids
     const int *n2ePtr;   // n+1
     const int *n2e;      // node -> face ids (one entry per occurrence)
+    int nFaces = 0;
+    double *faceScratch = nullptr;  // 8 per face: area and unit normal of the current surface (4 nFaces),
+                                    // then their adjoints (4 nFaces)
 };
 
 // Tree nodes in preorder.  info = (l, u, escape, isLeaf).

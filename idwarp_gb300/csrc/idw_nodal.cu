@@ -248,6 +248,38 @@ __device__ void rotation_matrix_b(const double *v1, const double *v2, const doub
     v2b[2] += vv2b[2] / mag2 + tmp[2] + v2[2] * mag2b / mag2;
 }
 
+// Area and unit normal of every face of the current surface, once per face
+// (the node kernels read them instead of recomputing each face per node).
+__global__ void k_face_props(SurfaceDev s, const double *Xu) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= s.nFaces) return;
+    const int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
+    double area, fn[3];
+    element_props(Xu, s.faceConn + f0, np, area, fn);
+    double *o = s.faceScratch + 4 * int64_t(f);
+    o[0] = area;
+    o[1] = fn[0];
+    o[2] = fn[1];
+    o[3] = fn[2];
+}
+
+// Area-weighted node normal from the stored face properties, summed over the
+// node's faces in the order of node_normal.
+__device__ void node_normal_f(const SurfaceDev &s, int i, double &sumArea, double *sumNormal) {
+    sumArea = 0.0;
+    sumNormal[0] = sumNormal[1] = sumNormal[2] = 0.0;
+    for (int e = s.n2ePtr[i]; e < s.n2ePtr[i + 1]; ++e) {
+        const int f = s.n2e[e];
+        const int np = s.facePtr[f + 1] - s.facePtr[f];
+        const double *fp = s.faceScratch + 4 * int64_t(f);
+        const double dA = fp[0] / double(np);
+        sumArea += dA;
+        sumNormal[0] += dA * fp[1];
+        sumNormal[1] += dA * fp[2];
+        sumNormal[2] += dA * fp[3];
+    }
+}
+
 // Area-weighted node normal from the node's faces (kd_tree.F90:1603-1625).
 __device__ void node_normal(const SurfaceDev &s, const double *Xu, int i, double &sumArea, double *sumNormal) {
     sumArea = 0.0;
@@ -315,7 +347,7 @@ __global__ void k_nodal(SurfaceDev s, const double *Xu, const dbl4 *xa, const do
     if (Ai[i] != 0.0) {
         if (useRotations && !isCorner[i]) {
             double sa, sn[3];
-            node_normal(s, Xu, i, sa, sn);
+            node_normal_f(s, i, sa, sn);
             double nrm[3] = {sn[0] / sa, sn[1] / sa, sn[2] / sa};
             rotation_matrix(normals0 + 3 * i, nrm, M);
         }
@@ -413,16 +445,21 @@ __global__ void k_set_data_b(TreeDev t, const double *nodeAdj, double *ptAdj, in
 // node, scatter to face vertices with atomics.
 // relative = 1: ptAdj's first nine entries already hold Mib - Xu0 (x) Bib
 // (the mixed adjoint accumulates them that way).
-__global__ void k_nodal_b(SurfaceDev s, const double *Xu, const dbl4 *xa, const double *normals0,
-                          const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub) {
+// Reverse nodal properties, node part (COMPUTENODALPROPERTIES_B): Xub += Bb;
+// for a rotating node, Mb through the Rodrigues adjoint to the node normal,
+// and from it the adjoints of the face areas and normals it was summed from,
+// added per face (the face part then runs each face's element adjoint once:
+// element_props_b is linear in those adjoints).
+__global__ void k_nodal_b_nodes(SurfaceDev s, const dbl4 *xa, const double *normals0, const int *isCorner,
+                                int useRotations, const double *ptAdj, int relative, double *Xub) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= s.n) return;
     const double *adj = ptAdj + 12 * i;
     double Mb[9];
     double Bb[3] = {adj[9], adj[10], adj[11]};
-    atomicAdd(Xub + 3 * i + 0, Bb[0]);
-    atomicAdd(Xub + 3 * i + 1, Bb[1]);
-    atomicAdd(Xub + 3 * i + 2, Bb[2]);
+    Xub[3 * i + 0] += Bb[0];
+    Xub[3 * i + 1] += Bb[1];
+    Xub[3 * i + 2] += Bb[2];
     if (!(useRotations && !isCorner[i])) return;
     const int e0 = s.n2ePtr[i], e1 = s.n2ePtr[i + 1];
     if (e1 == e0) return;
@@ -433,22 +470,37 @@ __global__ void k_nodal_b(SurfaceDev s, const double *Xu, const dbl4 *xa, const 
 #pragma unroll
         for (int k = 0; k < 3; ++k) Mb[3 * a + k] = relative ? adj[3 * a + k] : adj[3 * a + k] - x0[k] * Bb[a];
     double sa, sn[3];
-    node_normal(s, Xu, i, sa, sn);
+    node_normal_f(s, i, sa, sn);
     double nrm[3] = {sn[0] / sa, sn[1] / sa, sn[2] / sa};
     double nb[3] = {0, 0, 0};
     rotation_matrix_b(normals0 + 3 * i, nrm, Mb, nb);
     double snb[3] = {nb[0] / sa, nb[1] / sa, nb[2] / sa};
     double sab = -(sn[0] * nb[0] + sn[1] * nb[1] + sn[2] * nb[2]) / sa / sa;
+    double *faceAdj = s.faceScratch + 4 * int64_t(s.nFaces);
     for (int e = e1 - 1; e >= e0; --e) {
-        int f = s.n2e[e];
-        int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
-        double area, fn[3];
-        element_props(Xu, s.faceConn + f0, np, area, fn);
-        double dA = area / double(np);
-        double dAb = sab + fn[0] * snb[0] + fn[1] * snb[1] + fn[2] * snb[2];
-        double fnb[3] = {dA * snb[0], dA * snb[1], dA * snb[2]};
-        element_props_b(Xu, s.faceConn + f0, np, dAb / double(np), fnb, Xub);
+        const int f = s.n2e[e];
+        const int np = s.facePtr[f + 1] - s.facePtr[f];
+        const double *fp = s.faceScratch + 4 * int64_t(f);
+        const double dA = fp[0] / double(np);
+        const double dAb = sab + fp[1] * snb[0] + fp[2] * snb[1] + fp[3] * snb[2];
+        double *fa = faceAdj + 4 * int64_t(f);
+        atomicAdd(fa + 0, dAb / double(np));
+        atomicAdd(fa + 1, dA * snb[0]);
+        atomicAdd(fa + 2, dA * snb[1]);
+        atomicAdd(fa + 3, dA * snb[2]);
     }
+}
+
+// Reverse nodal properties, face part: each face's element adjoint with the
+// summed area and normal adjoints of its nodes, into Xub of its vertices.
+__global__ void k_nodal_b_faces(SurfaceDev s, const double *Xu, double *Xub) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= s.nFaces) return;
+    const double *fa = s.faceScratch + 4 * int64_t(s.nFaces) + 4 * int64_t(f);
+    const double areab = fa[0], nb[3] = {fa[1], fa[2], fa[3]};
+    if (areab == 0.0 && nb[0] == 0.0 && nb[1] == 0.0 && nb[2] == 0.0) return;
+    const int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
+    element_props_b(Xu, s.faceConn + f0, np, areab, nb, Xub);
 }
 
 // dXs[XuInd[i]] = Xub[i]: only the first caller occurrence of a unique point
@@ -633,8 +685,9 @@ void launch_corners(const SurfaceDev &s, const double *Xu, const double *normals
 }
 void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
                   const double *Ai, const int *isCorner, int useRotations, double *ptMB, cudaStream_t st) {
-    if (s.n > 0)
-        k_nodal<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, Ai, isCorner, useRotations, ptMB);
+    if (s.n <= 0) return;
+    if (useRotations && s.nFaces > 0) k_face_props<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu);
+    k_nodal<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, Ai, isCorner, useRotations, ptMB);
 }
 void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, const SetDataScratch &sc, cudaStream_t st) {
     if (t.nNodes <= 0) return;
@@ -650,9 +703,13 @@ void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, i
 void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
                     const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
                     cudaStream_t st) {
-    if (s.n > 0)
-        k_nodal_b<<<blocks(s.n, 128), 128, 0, st>>>(s, Xu, xa, normals0, isCorner, useRotations, ptAdj, relative,
-                                                    Xub);
+    if (s.n <= 0) return;
+    if (useRotations && s.nFaces > 0) {
+        k_face_props<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu);
+        cudaMemsetAsync(s.faceScratch + 4 * size_t(s.nFaces), 0, 4 * sizeof(double) * size_t(s.nFaces), st);
+    }
+    k_nodal_b_nodes<<<blocks(s.n, 128), 128, 0, st>>>(s, xa, normals0, isCorner, useRotations, ptAdj, relative, Xub);
+    if (useRotations && s.nFaces > 0) k_nodal_b_faces<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu, Xub);
 }
 void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,
                     const double *Ai, const int *isCorner, int useRotations, int plusIdentity, double *ptMBd,
