@@ -84,3 +84,16 @@ def test_tiled_exact_matches_oracle_with_gate_forced(built_lib, oracle_lib):
     x, st = _warp(m, {"mixedGate": 1e-6, "exactSchedule": "tiled"})
     assert st["preciseTerms"] > 0
     assert np.abs(x.reshape(-1, 3) - xo).max() / om.ldef0() < 1e-9
+
+
+def test_tiled_exact_tangent_equals_walk(built_lib):
+    # warpDerivFwd in exact mode runs the same evaluation with the tangent
+    # nodal properties: the tiled schedule gives the walk's bits
+    m = wing_small()
+    dxs = np.random.default_rng(61).normal(size=m["pts"].shape)
+    out = {}
+    for sched in ("tiled", "walk"):
+        g = build_gpu(m, {"evalMode": "exact", "exactSchedule": sched}, precision="mixed")
+        g.setSurfaceCoordinates(m["xs"])
+        out[sched] = g.warpDerivFwd(dxs, solverVec=False)
+    np.testing.assert_array_equal(out["tiled"], out["walk"])
