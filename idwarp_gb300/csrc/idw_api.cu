@@ -1129,7 +1129,7 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
         if (!mixed) launch_set_data_b(tree_dev(c), nodeAdj.p + size_t(sd) * 12 * nn, pa, n, c->stream);
         CK(cudaMemsetAsync(c->xub.p, 0, sizeof(double) * 3 * n, c->stream));
         launch_nodal_b(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa, mixed,
-                       c->xub.p, c->stream);
+                       c->xub.p, c->stream, sd == 0);
         double *dst = (where == IDW_DEVICE) ? dxsOut + sd * dxsStride : c->dxs.p;
         CK(cudaMemsetAsync(dst, 0, sizeof(double) * 3 * c->nPts, c->stream));
         launch_scatter_dxs(n, c->xuInd.p, c->xub.p, dst, c->stream);

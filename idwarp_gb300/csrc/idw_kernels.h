@@ -129,9 +129,10 @@ void launch_nodal(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const d
 void launch_set_data(const TreeDev &t, const double *ptMB, double *nodeMB, const SetDataScratch &sc, cudaStream_t st);
 void launch_tree_parents(const TreeDev &t, int *parent, cudaStream_t st);
 void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, int nPts, cudaStream_t st);
+// faceProps = 0 reuses the face areas and normals of the previous call (same surface)
 void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
                     const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
-                    cudaStream_t st);
+                    cudaStream_t st, int faceProps = 1);
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st);
 // Tangent nodal properties: (Md [+ I], bd) per point, 12 doubles (M row-major, b).
 void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,

@@ -702,10 +702,10 @@ void launch_set_data_b(const TreeDev &t, const double *nodeAdj, double *ptAdj, i
 }
 void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
                     const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
-                    cudaStream_t st) {
+                    cudaStream_t st, int faceProps) {
     if (s.n <= 0) return;
     if (useRotations && s.nFaces > 0) {
-        k_face_props<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu);
+        if (faceProps) k_face_props<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu);
         cudaMemsetAsync(s.faceScratch + 4 * size_t(s.nFaces), 0, 4 * sizeof(double) * size_t(s.nFaces), st);
     }
     k_nodal_b_nodes<<<blocks(s.n, 128), 128, 0, st>>>(s, xa, normals0, isCorner, useRotations, ptAdj, relative, Xub);
