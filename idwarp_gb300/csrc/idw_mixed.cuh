@@ -123,12 +123,6 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
     e = fmaf(a.l, b.h, e);
     return df_norm(p, e);
 }
-__device__ __forceinline__ dfl df_mulf(dfl a, float b) {
-    const float p = a.h * b;
-    float e = fmaf(a.h, b, -p);
-    e = fmaf(a.l, b, e);
-    return df_norm(p, e);
-}
 // 1/sqrt(q) with one Newton step carried in double-float.
 __device__ __forceinline__ dfl df_rsqrt(dfl q) {
     const float y0 = rsqrtf(q.h);
