@@ -1,11 +1,14 @@
 /* A C caller of libidwarp_gb300.so (include/idwarp_gb300.h): a cube surface
  * and a shell of volume points, surface definition through idw_point_reduce,
  * a rigid translation warp (every volume node must move by the translation)
- * and the translation identity of the reverse product (sum dXs = sum dXv).
- * Exit status 0 on success. */
+ * and the translation identity of the reverse product (sum dXs = sum dXv);
+ * then the restart-file path: a second context loads the first one's
+ * denominator estimate (a tampered copy is refused) and warps to the same
+ * bits.  Exit status 0 on success. */
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "idwarp_gb300.h"
 
@@ -109,7 +112,31 @@ int main(void) {
     for (int k = 0; k < 3 * npts; ++k) sum += dxs[k];
     idw_stats st;
     check(ctx, idw_get_stats(ctx, &st), "get_stats");
+
+    /* restart: the estimate and the dryRun costs of this context ... */
+    double *den0 = malloc(sizeof(double) * nvol), *costs = malloc(sizeof(double) * nvol);
+    check(ctx, idw_get_denominator0(ctx, den0, nvol, IDW_HOST), "get_denominator0");
+    check(ctx, idw_dry_run_costs(ctx, costs, nvol, IDW_HOST), "dry_run_costs");
     idw_destroy(ctx);
+    for (int i = 0; i < nvol; ++i)
+        if (!(costs[i] > 0.0)) return 6;
+    /* ... loaded by a second one in place of computing it */
+    void *ctx2 = NULL;
+    if (idw_create(&o, &ctx2) != IDW_OK) { fprintf(stderr, "idw_create failed\n"); return 1; }
+    check(ctx2, idw_create_common_grid(ctx2, xv0, nvol, IDW_HOST), "create_common_grid (2)");
+    check(ctx2, idw_set_symmetry_planes(ctx2, NULL, NULL, 0), "set_symmetry_planes (2)");
+    check(ctx2, idw_initialize_warping(ctx2, pts, npts, sorted, nu, link, fs, nfaces, conn, 4 * nfaces),
+          "initialize_warping (2)");
+    den0[0] *= 2.0; /* node 0 is checked: an estimate above the truth is refused */
+    if (idw_set_denominator0(ctx2, den0, nvol, 100, IDW_HOST) != IDW_ERR_RESTART) return 4;
+    den0[0] *= 0.5;
+    check(ctx2, idw_set_denominator0(ctx2, den0, nvol, 100, IDW_HOST), "set_denominator0");
+    check(ctx2, idw_set_surface_coordinates(ctx2, xs, 3 * npts, IDW_HOST), "set_surface_coordinates (2)");
+    check(ctx2, idw_warp_mesh(ctx2), "warp_mesh (2)");
+    double *xv2 = malloc(sizeof(double) * 3 * nvol);
+    check(ctx2, idw_get_volume_coordinates(ctx2, xv2, 3 * nvol, IDW_HOST), "get_volume_coordinates (2)");
+    idw_destroy(ctx2);
+    if (memcmp(xv, xv2, sizeof(double) * 3 * nvol) != 0) return 5;
     printf("nvol %d nunique %d translation error %.3e sum(dXs) %.12g expected %d leafPairs %lld\n", nvol, nu, err,
            sum, 3 * nvol, (long long)st.leafPairs);
     if (!(err < 1e-12)) return 2;
