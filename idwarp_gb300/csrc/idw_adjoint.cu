@@ -26,7 +26,10 @@ template <int S>
 struct AdjSmem {
     static constexpr int kChunk = S <= 4 ? 10 : 8;
     float nb[32][3 * S];       // seeds of every lane (numerator adjoints, scaled)
-    float4 vb[kChunk][32];     // per point: w, w (r - C)
+    // per point: w, w (r - C); for 8 seeds the rows are padded so that lane
+    // groups reading different points hit different banks
+    static constexpr int kRow = S == 8 ? 33 : 32;
+    float4 vb[kChunk][kRow];
 };
 
 // Lands the four moment sums of term `target`, seed component c (seed s, axis
@@ -79,6 +82,48 @@ __device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *t
             }
         }
     }
+    __syncwarp();
+}
+
+// Leaf chunks for 8 seeds: lane group g = lane / S (32 / S groups) takes
+// every (32/S)-th point of the chunk, lane s = lane % S all three axes of seed
+// s, so all 32 lanes work where the blocked form keeps 24 (13% faster at 8M
+// nodes; for 16 seeds the blocked form measured faster and stays).
+template <int S>
+__device__ __forceinline__ void reduce_groups(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
+    constexpr int G = 32 / S;
+    constexpr int P = (AdjSmem<S>::kChunk + G - 1) / G;
+    const int lane = threadIdx.x & 31;
+    const int s = lane % S, g = lane / S;
+    __syncwarp();
+    float acc[P][3][4];
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[q][a][0] = acc[q][a][1] = acc[q][a][2] = acc[q][a][3] = 0.f;
+    for (int l = 0; l < 32; ++l) {
+        const float n[3] = {sm.nb[l][3 * s], sm.nb[l][3 * s + 1], sm.nb[l][3 * s + 2]};
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            if (g + G * q < m) {
+                const float4 v = sm.vb[g + G * q][l];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    acc[q][a][0] = fmaf(v.x, n[a], acc[q][a][0]);
+                    acc[q][a][1] = fmaf(v.y, n[a], acc[q][a][1]);
+                    acc[q][a][2] = fmaf(v.z, n[a], acc[q][a][2]);
+                    acc[q][a][3] = fmaf(v.w, n[a], acc[q][a][3]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+        if (g + G * q < m)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                land_moments(adj, seedStride, 3 * s + a, base + g + G * q, acc[q][a][0], acc[q][a][1], acc[q][a][2],
+                             acc[q][a][3]);
     __syncwarp();
 }
 
@@ -226,7 +271,7 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         const int m = min(kChunk, inf.y - i0 + 1);
                         for (int p = 0; p < m; ++p) {
                             const int i = i0 + p;
-                            if (S >= 8) targets[p] = i;
+                            if (S >= 16) targets[p] = i;
                             float w = 0.f;
                             if (active) {
                                 const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
@@ -241,6 +286,8 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         }
                         if constexpr (S <= 4)
                             reduce_tasks<S>(sm, m, i0, ptAdj, ptStride);
+                        else if constexpr (S == 8)
+                            reduce_groups<S>(sm, m, i0, ptAdj, ptStride);
                         else
                             reduce_terms<S>(sm, m, targets, ptAdj, ptStride);
                     }
