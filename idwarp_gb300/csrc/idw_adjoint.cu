@@ -15,6 +15,7 @@
 // seeds, which the warp forms from shared memory; one FP64 atomic per result
 // lands it in the per-point / per-cluster accumulators.
 #include "idw_mixed.cuh"
+#include "idwarp_gb300.h"
 
 namespace idw {
 
@@ -154,40 +155,15 @@ __device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, do
 }
 
 // One seed, one term: the 12 products v (x) n of every lane summed over the
-// warp with shuffles.  Two halving exchanges (xor 16, 8) leave lane group
-// G = lane >> 3 with the 3 products of moment G; three butterflies (xor 4, 2,
-// 1) complete the sums; lanes 0..2 of each group land them.  Called by all 32
-// lanes.
+// warp (warp_land_moments).  Called by all 32 lanes.
 __device__ __forceinline__ void reduce_one_s1(const float4 v, const float n[3], double *d) {
-    const int lane = threadIdx.x & 31;
     const float vc[4] = {v.x, v.y, v.z, v.w};
     float P[12];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int a = 0; a < 3; ++a) P[3 * k + a] = vc[k] * n[a];
-    const bool h16 = lane & 16, h8 = lane & 8;
-    float Q[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const float send = h16 ? P[k] : P[k + 6];
-        Q[k] = (h16 ? P[k + 6] : P[k]) + __shfl_xor_sync(kFull, send, 16);
-    }
-    float R[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float send = h8 ? Q[k] : Q[k + 3];
-        R[k] = (h8 ? Q[k + 3] : Q[k]) + __shfl_xor_sync(kFull, send, 8);
-    }
-#pragma unroll
-    for (int o = 4; o; o >>= 1)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) R[k] += __shfl_xor_sync(kFull, R[k], o);
-    const int G = lane >> 3, a = lane & 7;
-    if (a < 3) {
-        const float val = a == 0 ? R[0] : (a == 1 ? R[1] : R[2]);
-        if (val != 0.f) atomicAdd(d + (G == 0 ? 9 + a : 3 * a + G - 1), double(val));
-    }
+    warp_land_moments(P, d);
 }
 
 template <int S, int KIND>
@@ -274,13 +250,9 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                             if (S >= 16) targets[p] = i;
                             float w = 0.f;
                             if (active) {
-                                const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
-                                const float dx = (h0 - da.x) + (l0 - dl.x);
-                                const float dy = (h1 - da.y) + (l1 - dl.y);
-                                const float dz = (h2 - da.z) + (l2 - dl.z);
-                                const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
-                                const float r1 = rsqrt_normal(d2);
-                                w = da.w * law.eval(fmaf(Ls, r1, LsLo * r1), c1, ab, abl);
+                                float dx, dy, dz;
+                                w = leaf_weight<KIND>(law, Ls, LsLo, c1, ab, abl, h0, h1, h2, l0, l1, l2,
+                                                      ldgf4(pf.da + i), ldgf4(pf.dl + i), dx, dy, dz);
                             }
                             sm.vb[p][lane] = make_float4(w, w * R0, w * R1, w * R2);
                         }
@@ -415,6 +387,12 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
     const int64_t ptStride = 12 * int64_t(nPts), nodeStride = 12 * int64_t(t.nNodes);
     // no volume nodes: no walk, the combination below writes zero adjoints
     int s0 = v.nVol > 0 ? 0 : nSeeds;
+    // exact mode on a mesh that fills the GPU: seeds that would walk alone go
+    // through the tiled kernel (2.6x the one-seed walk on the 2M-node wing);
+    // groups of 4, 8 or 16 keep the shared walk (16 seeds: 4.7 s against 16
+    // tiled passes, 5.8 s)
+    const bool tiledOne = exact && tf.nLeaves > 0 && k.exactSchedule != IDW_EXACT_WALK &&
+                          (k.exactSchedule == IDW_EXACT_TILED || exact_tiled_fills(v.nVol));
     while (s0 < nSeeds) {
         const int left = nSeeds - s0;
         const double *d = dxv + s0 * dxvStride;
@@ -432,6 +410,9 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
             launch_adj_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
                               counters, st);
             s0 += 4;
+        } else if (tiledOne) {
+            launch_exact_adjoint(tf, pf, v, rec, mp, k.law, d, den, pa, counters, st);
+            s0 += 1;
         } else {
             launch_adj_law<1>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
                               counters, st);

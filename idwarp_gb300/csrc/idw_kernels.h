@@ -169,6 +169,12 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
 void launch_exact_mixed(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, const VolumeDev &v,
                         const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, float4 *acc,
                         unsigned long long *counters, cudaStream_t st);
+// Exact-mode reverse product of one seed (dxv: 3 per volume node, common
+// order) into the points' relative moments ptAdj (12 per point, zeroed by the
+// caller), tiled as launch_exact_mixed (idw_exact.cu).
+void launch_exact_adjoint(const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
+                          const MixedParams &mp, const WeightLaw &wl, const double *dxv, const double *den,
+                          double *ptAdj, unsigned long long *counters, cudaStream_t st);
 // True when the tiled exact kernel has volume nodes for at least two full
 // waves of the device (below that the walk's finer grain is faster).
 bool exact_tiled_fills(int64_t nVol);

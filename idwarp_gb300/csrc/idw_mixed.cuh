@@ -314,6 +314,38 @@ __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const Volume
     return dec;
 }
 
+// The warp's sum of the 12 moment products P[3 k + a] (k = 0: w, k = 1..3:
+// w (r - C)_k; a the seed axis) of every lane, landed in one term's adjoint
+// accumulator d (slots 9 + a for w, 3 a + k - 1 for the moments).  Two
+// halving exchanges (xor 16, 8) leave lane group G = lane >> 3 with the 3
+// products of moment G; three butterflies (xor 4, 2, 1) complete the sums;
+// lanes 0..2 of each group land them.  Called by all 32 lanes.
+__device__ __forceinline__ void warp_land_moments(const float *P, double *d) {
+    const int lane = threadIdx.x & 31;
+    const bool h16 = lane & 16, h8 = lane & 8;
+    float Q[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const float send = h16 ? P[k] : P[k + 6];
+        Q[k] = (h16 ? P[k + 6] : P[k]) + __shfl_xor_sync(kFull, send, 16);
+    }
+    float R[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float send = h8 ? Q[k] : Q[k + 3];
+        R[k] = (h8 ? Q[k + 3] : Q[k]) + __shfl_xor_sync(kFull, send, 8);
+    }
+#pragma unroll
+    for (int o = 4; o; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) R[k] += __shfl_xor_sync(kFull, R[k], o);
+    const int G = lane >> 3, a = lane & 7;
+    if (a < 3) {
+        const float val = a == 0 ? R[0] : (a == 1 ? R[1] : R[2]);
+        if (val != 0.f) atomicAdd(d + (G == 0 ? 9 + a : 3 * a + G - 1), double(val));
+    }
+}
+
 // Power of two 2^e as a float (|e| <= 126).
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + max(-126, min(127, e))) << 23); }
 
@@ -361,18 +393,27 @@ __device__ __forceinline__ float rsqrt_normal(float x) {
 // One leaf pair in FP32 (evalNodeExact's term, kd_tree.F90:664-690): h + l
 // is r - C (leaf centroid), da + dl the point's offset from C and its area,
 // m0..m2 the point's D' (row-major, 9) and u' (3); accumulates w S and w.
+// The weight of one leaf pair (and the pair's offset dx, dy, dz).
+template <int KIND>
+__device__ __forceinline__ float leaf_weight(const Law32<KIND> &law, float Ls, float LsLo, float c1, float ab,
+                                             float abl, float h0, float h1, float h2, float l0, float l1, float l2,
+                                             const float4 da, const float4 dl, float &dx, float &dy, float &dz) {
+    dx = (h0 - da.x) + (l0 - dl.x);
+    dy = (h1 - da.y) + (l1 - dl.y);
+    dz = (h2 - da.z) + (l2 - dl.z);
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
+    const float r1 = rsqrt_normal(d2);
+    const float tt = fmaf(Ls, r1, LsLo * r1);
+    return da.w * law.eval(tt, c1, ab, abl);
+}
+
 template <int KIND>
 __device__ __forceinline__ void leaf_pair(const Law32<KIND> &law, float Ls, float LsLo, float c1, float ab,
                                           float abl, float h0, float h1, float h2, float l0, float l1, float l2,
                                           const float4 da, const float4 dl, const float4 m0, const float4 m1,
                                           const float4 m2, float &pn0, float &pn1, float &pn2, float &pd) {
-    const float dx = (h0 - da.x) + (l0 - dl.x);
-    const float dy = (h1 - da.y) + (l1 - dl.y);
-    const float dz = (h2 - da.z) + (l2 - dl.z);
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, 1e-15f)));
-    const float r1 = rsqrt_normal(d2);
-    const float tt = fmaf(Ls, r1, LsLo * r1);
-    const float w = da.w * law.eval(tt, c1, ab, abl);
+    float dx, dy, dz;
+    const float w = leaf_weight<KIND>(law, Ls, LsLo, c1, ab, abl, h0, h1, h2, l0, l1, l2, da, dl, dx, dy, dz);
     // S = D dx + u ; D row-major in m0.xyzw m1.xyzw m2.x, u in m2.yzw
     const float S0 = fmaf(m0.x, dx, fmaf(m0.y, dy, fmaf(m0.z, dz, m2.y)));
     const float S1 = fmaf(m0.w, dx, fmaf(m1.x, dy, fmaf(m1.y, dz, m2.z)));

@@ -97,3 +97,37 @@ def test_tiled_exact_tangent_equals_walk(built_lib):
         g.setSurfaceCoordinates(m["xs"])
         out[sched] = g.warpDerivFwd(dxs, solverVec=False)
     np.testing.assert_array_equal(out["tiled"], out["walk"])
+
+
+def _deriv(m, opts, precision, dxv):
+    g = build_gpu(m, dict(opts, evalMode="exact"), precision=precision)
+    g.setSurfaceCoordinates(m["xs"])
+    g.warpMesh()
+    if dxv.ndim == 1:
+        g.warpDeriv(dxv, solverVec=False)
+        return g.getdXs()
+    return g.warpDerivBatch(dxv)
+
+
+@pytest.mark.parametrize("which,planes", [("wing", 0), ("sphere", 3)])
+def test_tiled_exact_adjoint(which, planes, built_lib):
+    # the reverse product in exact mode: tiled (per-warp moment reduction)
+    # against the walk and against the FP64 form; sums in another order, so
+    # within the mixed form's tolerance rather than bitwise
+    m = _mesh(which, planes)
+    dxv = np.random.default_rng(71).normal(size=3 * len(m["xv0"]))
+    ref = _deriv(m, {}, "fp64", dxv)
+    tiled = _deriv(m, {"exactSchedule": "tiled"}, "mixed", dxv)
+    walk = _deriv(m, {"exactSchedule": "walk"}, "mixed", dxv)
+    scale = np.abs(ref).max()
+    assert np.abs(tiled - walk).max() <= 1e-6 * scale
+    assert np.abs(tiled - ref).max() <= 1e-6 * scale
+
+
+def test_tiled_exact_adjoint_several_seeds(built_lib):
+    m = wing_small()
+    dxv = np.random.default_rng(72).normal(size=(3, len(m["xv0"]), 3))
+    tiled = _deriv(m, {"exactSchedule": "tiled"}, "mixed", dxv)
+    walk = _deriv(m, {"exactSchedule": "walk"}, "mixed", dxv)
+    assert tiled.shape == walk.shape
+    assert np.abs(tiled - walk).max() <= 1e-6 * np.abs(walk).max()
