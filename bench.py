@@ -303,7 +303,7 @@ def run_suite():
                     res["%s_%s_ms" % (mode, prec)] = ms
                     res["%s_%s_nodes_per_s" % (mode, prec)] = nvol / (ms * 1e-3)
                     res["%s_PI" % mode] = st["leafPairs"] + st["approx"]
-                    if mode == "fast" and errTol == 1e-4 and name != "P_wing_8M":
+                    if errTol == 1e-4 and name != "P_wing_8M" and (mode == "fast" or prec == "mixed"):
                         rng = np.random.default_rng(1)
                         seed = torch.tensor(rng.normal(size=3 * nvol), device="cuda")
                         dxs = torch.empty(3 * len(m["pts"]), dtype=torch.float64, device="cuda")
@@ -312,7 +312,7 @@ def run_suite():
                             g.lib.idw_warp_deriv_batch(g.ctx, C.c_void_p(seed.data_ptr()), 1, C.c_void_p(dxs.data_ptr()),
                                                        _lib.IDW_DEVICE)
 
-                        res["warpDeriv1_%s_ms" % prec] = _timed(deriv, 2, stream)
+                        res["warpDeriv1_%s_%s_ms" % (mode, prec)] = _timed(deriv, 2, stream)
                     del g
                 Ldef = None
             # precision error (same tree, same decisions) and algorithmic error
