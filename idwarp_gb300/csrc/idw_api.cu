@@ -878,8 +878,27 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
     if (rc) return rc;
     rec.gden = c->gden.p;
     CK(cudaEventRecord(c->ev0, c->stream));
-    launch_walk_mixed_batch(nb, tree_dev(c), tf, pf, 12 * int64_t(n), af, 12 * int64_t(nn), int64_t(nn), vol_dev(c),
-                            rec, k, exact, c->bAcc.p, 2 * c->nVol, c->counters.p, c->stream);
+    if (exact && tf.nLeaves > 0 && k.exactSchedule != IDW_EXACT_WALK &&
+        (k.exactSchedule == IDW_EXACT_TILED || exact_tiled_fills(c->nVol))) {
+        // exact mode on a mesh that fills the GPU: the tiled kernel per surface
+        // (no decisions to share between surfaces)
+        const MixedParams mp = make_mixed_params(k);
+        for (int b = 0; b < nb; ++b) {
+            PointsDevF pb = pf;
+            pb.dm += size_t(b) * 12 * n;
+            pb.dml += size_t(b) * 12 * n;
+            NodeAggF ab = af;
+            ab.dc += size_t(b) * 12 * nn;
+            ab.dcl += size_t(b) * 12 * nn;
+            ab.dn += size_t(b) * nn;
+            ab.ref += 24 * b;
+            launch_exact_mixed(tf, pb, ab, vol_dev(c), rec, mp, k.law, c->bAcc.p + size_t(b) * 2 * c->nVol,
+                               c->counters.p, c->stream);
+        }
+    } else {
+        launch_walk_mixed_batch(nb, tree_dev(c), tf, pf, 12 * int64_t(n), af, 12 * int64_t(nn), int64_t(nn),
+                                vol_dev(c), rec, k, exact, c->bAcc.p, 2 * c->nVol, c->counters.p, c->stream);
+    }
     for (int b = 0; b < nb; ++b)
         launch_finalize_mixed(vol_dev(c), rec, c->bAcc.p + size_t(b) * 2 * c->nVol, k.law.bExp,
                               outDev + size_t(b) * vdof, c->stream, tangent);

@@ -131,3 +131,18 @@ def test_tiled_exact_adjoint_several_seeds(built_lib):
     walk = _deriv(m, {"exactSchedule": "walk"}, "mixed", dxv)
     assert tiled.shape == walk.shape
     assert np.abs(tiled - walk).max() <= 1e-6 * np.abs(walk).max()
+
+
+def test_tiled_exact_batch_equals_single_warps(built_lib):
+    # warpMeshBatch in exact mode runs the tiled kernel once per surface: the
+    # same bits as one warpMesh per surface
+    from idwarp_gb300 import synthetic as S
+
+    m = wing_small()
+    surf = np.stack([S.wing_perturbation(m["pts"], seed=300 + i) for i in range(3)])
+    g = build_gpu(m, {"evalMode": "exact", "exactSchedule": "tiled"}, precision="mixed")
+    batch = g.warpMeshBatch(surf)
+    for i in range(3):
+        g.setSurfaceCoordinates(surf[i])
+        g.warpMesh()
+        np.testing.assert_array_equal(batch[i].ravel(), g.getWarpGrid())
