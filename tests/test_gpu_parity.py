@@ -239,6 +239,23 @@ def test_mixed_denominator_feeds_deriv(wing, built_lib, oracle_lib):
     assert np.abs(g.getdXs() - do).max() <= 1e-6 * np.abs(do).max()
 
 
+def test_mixed_deriv_every_seed_group(wing, built_lib):
+    # 29 seeds = groups of 16, 8, 4 and 1: every form of the mixed adjoint's
+    # warp reduction (blocked, lane groups, per-task lanes, shuffles) against
+    # the FP64 adjoint
+    g64 = build_gpu(wing, precision="fp64")
+    g32 = build_gpu(wing, precision="mixed")
+    seeds = np.random.default_rng(19).normal(size=(29,) + wing["xv0"].shape)
+    out = []
+    for g in (g64, g32):
+        g.setSurfaceCoordinates(wing["xs"])
+        g.warpMesh()
+        out.append(g.warpDerivBatch(seeds))
+    for lo, hi in ((0, 16), (16, 24), (24, 28), (28, 29)):
+        ref = out[0][lo:hi]
+        assert np.abs(out[1][lo:hi] - ref).max() <= 1e-6 * np.abs(ref).max(), (lo, hi)
+
+
 @pytest.mark.parametrize("mode", ["fast", "exact"])
 def test_mixed_deriv_batch_matches_fp64(mode, wing, built_lib):
     # the mixed adjoint (S seeds sharing one walk) against the FP64 adjoint
