@@ -68,6 +68,15 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 __device__ __forceinline__ float4 ldgf4(const float4 *p) { return __ldg(p); }
 __device__ __forceinline__ int4 ldgi4(const int4 *p) { return __ldg(p); }
 
+// 1/sqrt(x) for an x that is normal or zero: the flush-to-zero form of the
+// approximate reciprocal square root gives the value rsqrtf gives, without
+// rsqrtf's handling of subnormal inputs.
+__device__ __forceinline__ float rsqrt_normal(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // FP32 error-table interpolation with a bound on its deviation from the FP64
 // value (see the file comment).  dOvrR >= 2 here.  The bracket index follows
 // the radii 2,3,4,5,7.5,10,20,40,...,640: unit steps below 5, then 7.5 and 10,
@@ -286,7 +295,10 @@ __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const floa
     rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
     rho2 = (rh[2] - ch.z) + (rl[2] - cl.z);
     d2 = fmaf(rho0, rho0, fmaf(rho1, rho1, rho2 * rho2));
-    rs = rsqrtf(d2);
+    // d2 is zero (a node on the centroid: dOvrR is NaN, the decision goes to
+    // FP64) or far above the subnormal range (the components are differences
+    // of hi/lo splits, resolved to ~1e-15), so the flush-to-zero form serves
+    rs = rsqrt_normal(d2);
     const float dOvrR = d2 * rs * ch.w;
     if (dOvrR < 2.0f * (1.0f - 4e-6f)) return 0;
     if (dOvrR <= 2.0f * (1.0f + 4e-6f)) return 2;
@@ -381,14 +393,6 @@ __device__ __forceinline__ NodeScale node_scale(const WalkRecF &rec, const Mixed
     return n;
 }
 
-// 1/sqrt(x) for a normal x (here x >= 1e-15): the flush-to-zero form of the
-// approximate reciprocal square root gives the value rsqrtf gives, without
-// rsqrtf's handling of subnormal inputs.
-__device__ __forceinline__ float rsqrt_normal(float x) {
-    float r;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
 
 // One leaf pair in FP32 (evalNodeExact's term, kd_tree.F90:664-690): h + l
 // is r - C (leaf centroid), da + dl the point's offset from C and its area,
