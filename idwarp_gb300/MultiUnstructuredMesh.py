@@ -163,3 +163,10 @@ class MultiUSMesh:
             raise Error("baseName is not optional for writeGrid")
         for name, mesh in zip(self.names, self.meshes):
             np.save("%s_%s.npy" % (baseName, name), mesh.getCommonGrid().reshape(-1, 3))
+
+    def __del__(self):
+        """Release the instances' device memory (MultiUnstructuredMesh.py:887-892):
+        each USMesh destroys its context."""
+        for mesh in getattr(self, "meshes", []):
+            mesh.__del__()
+        self.meshes = []
