@@ -168,5 +168,10 @@ class MultiUSMesh:
         """Release the instances' device memory (MultiUnstructuredMesh.py:887-892):
         each USMesh destroys its context."""
         for mesh in getattr(self, "meshes", []):
-            mesh.__del__()
+            release = getattr(mesh, "__del__", None)
+            if release is not None:
+                try:
+                    release()
+                except Exception:
+                    pass
         self.meshes = []
