@@ -540,7 +540,9 @@ def main():
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": int(xs_host.nbytes),
                 "d2h_bytes_per_step": int(grid.nbytes)},
         "clocks": clk,
-        "gpu_launches": 7 * args.steps,
+        # per step: gather_xu, face_props, nodal, set_data, mixed_nodal,
+        # mixed_nodes, walk, finalize
+        "gpu_launches": 8 * args.steps,
         "setup_s": setup_s,
         "work": {"leafPairs": st["leafPairs"], "approx": st["approx"], "visited": st["visited"],
                  "fp64Fallback": st["fp64Fallback"]},
