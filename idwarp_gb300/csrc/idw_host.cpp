@@ -3,7 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <unordered_map>
+#include <vector>
 
 namespace idw {
 
@@ -26,8 +26,11 @@ struct CellHash {
 
 int point_reduce(const double *pts, int n, double tol, double *uniquePts, int32_t *link) {
     if (n <= 0) return 0;
-    // Uniform hash grid with cells no smaller than tol, so every partner of a
-    // point lies in the 27 cells around it.
+    // Spatial hash with cells no smaller than tol, so every partner of a point
+    // lies in the 27 cells around it.  Buckets are linked lists of point
+    // indices in flat arrays (head per bucket, next per point); a bucket that
+    // other cells share only adds candidates, which the distance test rejects
+    // (points two cells apart are more than tol apart).
     double lo[3] = {pts[0], pts[1], pts[2]}, hi[3] = {pts[0], pts[1], pts[2]};
     for (int i = 0; i < n; ++i)
         for (int k = 0; k < 3; ++k) {
@@ -36,13 +39,19 @@ int point_reduce(const double *pts, int n, double tol, double *uniquePts, int32_
         }
     double ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-300});
     double h = std::max(tol, ext * std::ldexp(1.0, -40));
-    std::unordered_map<CellKey, std::vector<int32_t>, CellHash> grid;
-    grid.reserve(size_t(n) * 2);
-    auto cell = [&](const double *p) {
-        return CellKey{int64_t(std::floor((p[0] - lo[0]) / h)), int64_t(std::floor((p[1] - lo[1]) / h)),
-                       int64_t(std::floor((p[2] - lo[2]) / h))};
-    };
-    for (int i = 0; i < n; ++i) grid[cell(pts + 3 * i)].push_back(i);
+    std::vector<int64_t> cell(3 * size_t(n));
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) cell[3 * size_t(i) + k] = int64_t(std::floor((pts[3 * i + k] - lo[k]) / h));
+    size_t nb = 1;
+    while (nb < 2 * size_t(n)) nb <<= 1;
+    const CellHash hash;
+    auto bucket = [&](int64_t x, int64_t y, int64_t z) { return hash(CellKey{x, y, z}) & (nb - 1); };
+    std::vector<int32_t> head(nb, -1), next(n);
+    for (int i = 0; i < n; ++i) {
+        const size_t b = bucket(cell[3 * size_t(i)], cell[3 * size_t(i) + 1], cell[3 * size_t(i) + 2]);
+        next[i] = head[b];
+        head[b] = i;
+    }
     const double tol2 = tol * tol;
     std::memset(link, 0, sizeof(int32_t) * n);
     int nUnique = 0;
@@ -51,18 +60,15 @@ int point_reduce(const double *pts, int n, double tol, double *uniquePts, int32_
         const double *p = pts + 3 * i;
         ++nUnique;
         std::memcpy(uniquePts + 3 * (nUnique - 1), p, 3 * sizeof(double));
-        CellKey c = cell(p);
+        const int64_t *c = cell.data() + 3 * size_t(i);
         for (int dx = -1; dx <= 1; ++dx)
             for (int dy = -1; dy <= 1; ++dy)
-                for (int dz = -1; dz <= 1; ++dz) {
-                    auto it = grid.find(CellKey{c.x + dx, c.y + dy, c.z + dz});
-                    if (it == grid.end()) continue;
-                    for (int32_t j : it->second) {
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int32_t j = head[bucket(c[0] + dx, c[1] + dy, c[2] + dz)]; j >= 0; j = next[j]) {
                         const double *q = pts + 3 * j;
                         double ax = q[0] - p[0], ay = q[1] - p[1], az = q[2] - p[2];
                         if (ax * ax + ay * ay + az * az <= tol2) link[j] = nUnique;
                     }
-                }
     }
     return nUnique;
 }
