@@ -396,19 +396,13 @@ int idw_create_common_grid(void *ctx, const double *volnodes, int64_t nvol, int 
     int rc = copy_in(c, c->xv0.p, volnodes, 3 * size_t(nvol), where);
     if (rc) return rc;
     CK(cudaMemcpyAsync(c->xv.p, c->xv0.p, 3 * nvol * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-    // bounding box on the host (set-up only)
-    std::vector<double> h(3 * size_t(nvol));
-    CK(cudaMemcpyAsync(h.data(), c->xv0.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (!all_finite(h.data(), h.size())) return fail(c, IDW_ERR_NONFINITE, "non-finite volume coordinates");
+    // bounding box and finiteness on the device (set-up only)
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     if (nvol > 0) {
-        for (int k = 0; k < 3; ++k) lo[k] = hi[k] = h[k];
-        for (int64_t i = 0; i < nvol; ++i)
-            for (int k = 0; k < 3; ++k) {
-                lo[k] = std::min(lo[k], h[3 * i + k]);
-                hi[k] = std::max(hi[k], h[3 * i + k]);
-            }
+        int64_t nonFinite = 0;
+        if (volume_bbox(nvol, c->xv0.p, lo, hi, &nonFinite, c->stream))
+            return fail(c, IDW_ERR_CUDA, "volume bounding box failed");
+        if (nonFinite) return fail(c, IDW_ERR_NONFINITE, "non-finite volume coordinates");
         DevBuf<unsigned long long> codes, codesAlt;
         DevBuf<int> idx;
         CKA(codes.alloc(nvol));

@@ -149,6 +149,9 @@ int64_t launch_denominator0_strided(const TreeDev &t, const dbl4 *ptXA, const Vo
                                     const SymPlanes &sym, int64_t stride, double *out, cudaStream_t st);
 void launch_dry_run(const TreeDev &t, const VolumeDev &v, const SymPlanes &sym, double errTol, int nPts,
                     double *costs, cudaStream_t st);
+// Bounding box of n points on the device and the number of non-finite
+// coordinates (set-up; synchronises st).  Returns 0, or -1 on a CUDA error.
+int volume_bbox(int64_t n, const double *x, double *lo, double *hi, int64_t *nonFinite, cudaStream_t st);
 void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,
                          unsigned long long *codes, int *idx, cudaStream_t st);
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,

@@ -6,6 +6,7 @@
 //   dryRun         src/modules/kd_tree.F90:789-830, driven by src/warp/initializeWarping.F90:258-266
 #include <cub/cub.cuh>
 
+#include <cmath>
 #include <vector>
 
 #include "idw_common.cuh"
@@ -209,6 +210,43 @@ __global__ void k_dry_run(TreeDev t, VolumeDev v, SymPlanes sym, double errTol, 
     if (valid) costs[vi] = acc;
 }
 
+// Per-block bounding box and count of non-finite values of n points (3
+// doubles each), for the Morton codes: out[7 b .. 7 b + 2] minima, [+3 .. +5]
+// maxima, [+6] the count.  Minima and maxima are exact, so the box equals a
+// sequential scan's.
+__global__ void k_bbox(int64_t n, const double *x, double *out) {
+    __shared__ double s[7][256];
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, bad = 0.0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        for (int k = 0; k < 3; ++k) {
+            const double v = x[3 * i + k];
+            if (!isfinite(v)) {
+                bad += 1.0;
+            } else {
+                lo[k] = fmin(lo[k], v);
+                hi[k] = fmax(hi[k], v);
+            }
+        }
+    const int t = threadIdx.x;
+    for (int k = 0; k < 3; ++k) {
+        s[k][t] = lo[k];
+        s[3 + k][t] = hi[k];
+    }
+    s[6][t] = bad;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (t < w) {
+            for (int k = 0; k < 3; ++k) {
+                s[k][t] = fmin(s[k][t], s[k][t + w]);
+                s[3 + k][t] = fmax(s[3 + k][t], s[3 + k][t + w]);
+            }
+            s[6][t] += s[6][t + w];
+        }
+        __syncthreads();
+    }
+    if (t < 7) out[7 * int64_t(blockIdx.x) + t] = s[t][0];
+}
+
 __device__ __forceinline__ unsigned long long spread21(unsigned long long x) {
     x &= 0x1fffffull;
     x = (x | (x << 32)) & 0x1f00000000ffffull;
@@ -391,6 +429,32 @@ int64_t launch_denominator0_strided(const TreeDev &t, const dbl4 *ptXA, const Vo
 void launch_dry_run(const TreeDev &t, const VolumeDev &v, const SymPlanes &sym, double errTol, int nPts,
                     double *costs, cudaStream_t st) {
     if (v.nVol > 0 && nPts > 0) k_dry_run<<<blocks(v.nVol, 128), 128, 0, st>>>(t, v, sym, errTol, double(nPts), costs);
+}
+
+int volume_bbox(int64_t n, const double *x, double *lo, double *hi, int64_t *nonFinite, cudaStream_t st) {
+    const int nb = int(std::min<int64_t>(1024, std::max<int64_t>(1, (n + 255) / 256)));
+    double *dOut = nullptr;
+    if (cudaMalloc(&dOut, sizeof(double) * 7 * nb) != cudaSuccess) return -1;
+    k_bbox<<<nb, 256, 0, st>>>(n, x, dOut);
+    std::vector<double> h(7 * size_t(nb));
+    cudaError_t e = cudaMemcpyAsync(h.data(), dOut, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dOut);
+    if (e != cudaSuccess) return -1;
+    double bad = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = INFINITY;
+        hi[k] = -INFINITY;
+    }
+    for (int b = 0; b < nb; ++b) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::fmin(lo[k], h[7 * b + k]);
+            hi[k] = std::fmax(hi[k], h[7 * b + 3 + k]);
+        }
+        bad += h[7 * b + 6];
+    }
+    *nonFinite = int64_t(bad);
+    return 0;
 }
 
 void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,

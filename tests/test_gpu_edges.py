@@ -120,6 +120,22 @@ def test_mixed_derivatives_extreme_cases(opts, planes, built_lib):
         assert np.abs(out["mixed"][k] - ref).max() <= 1e-6 * np.abs(ref).max(), k
 
 
+def test_nonfinite_volume_grid_raises(sphere, built_lib):
+    # the volume grid's finiteness is checked on the device with its bounding box
+    import contextlib
+    import io
+
+    from idwarp_gb300 import USMesh
+    from idwarp_gb300._lib import LibraryError
+
+    x = np.array(sphere["xv0"], dtype=np.float64)
+    x[len(x) // 2, 1] = np.nan
+    with contextlib.redirect_stdout(io.StringIO()):
+        g = USMesh(options=dict(OPTS, fileType="NPY", precision="mixed"))
+    with pytest.raises(LibraryError, match="IDW_ERR_NONFINITE"):
+        g.createCommonGrid(x)
+
+
 def test_empty_volume_mesh(sphere, built_lib):
     import contextlib
     import io
