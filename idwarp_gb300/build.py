@@ -31,7 +31,7 @@ def _nvcc():
 def _flags():
     return ARCH + [
         "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-        "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE,
+        "--expt-relaxed-constexpr", "-Xcompiler", "-pthread", "-I", CSRC, "-I", INCLUDE,
     ]
 
 
@@ -83,7 +83,7 @@ def build(force=False, verbose=False, jobs=None):
             if verbose and msg:
                 print(msg)
     tmp = LIB + ".tmp"
-    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    link = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"]
     run(link)
     os.replace(tmp, LIB)
     with open(stamp, "w") as f:

@@ -4,6 +4,8 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
+#include <thread>
+#include <map>
 
 namespace idw {
 
@@ -111,69 +113,116 @@ void select_rank(const double *p, int32_t *perm, int c, int k, int lo, int hi) {
 
 }  // namespace
 
-void build_kdtree(const double *pts, int n, int bucket, FlatTree &t) {
-    t = FlatTree();
-    t.n = n;
-    t.bucket = bucket;
-    t.perm.resize(n);
-    for (int i = 0; i < n; ++i) t.perm[i] = i;
-    struct Item {
-        int l, u, depth, parentSlot;
-    };
-    // Preorder: pop a range, give it the next id, push right then left.
-    std::vector<Item> work;
-    work.push_back({0, n - 1, 1, -1});
-    std::vector<int32_t> rightChild;
-    while (!work.empty()) {
-        Item it = work.back();
-        work.pop_back();
-        int id = int(t.l.size());
-        t.l.push_back(it.l);
-        t.u.push_back(it.u);
-        t.depth.push_back(it.depth);
-        t.escape.push_back(-1);
-        rightChild.push_back(-1);
-        t.maxDepth = std::max(t.maxDepth, it.depth);
-        if (it.parentSlot >= 0) rightChild[it.parentSlot] = id;
-        if (it.u - it.l <= bucket) {
-            t.leaf.push_back(1);
-            continue;
+namespace {
+
+// Nodes of the subtree over m points: the split index (l+u)/2 gives the left
+// child (m-1)/2 + 1 points, so the count depends on m only.
+int subtree_nodes(int m, int bucket, std::map<int, int> &memo) {
+    if (m - 1 <= bucket) return 1;
+    auto it = memo.find(m);
+    if (it != memo.end()) return it->second;
+    const int left = (m - 1) / 2 + 1;
+    const int v = 1 + subtree_nodes(left, bucket, memo) + subtree_nodes(m - left, bucket, memo);
+    memo[m] = v;
+    return v;
+}
+
+struct KdBuild {
+    const double *pts;
+    int bucket;
+    FlatTree &t;
+    const std::map<int, int> &nodes;  // subtree node counts, filled before the build
+    int count(int m) const { return m - 1 <= bucket ? 1 : nodes.at(m); }
+
+    // Node id over ranks [l, u]; its subtree takes preorder ids
+    // [id, id + count(u - l + 1)), left child id + 1, right child after the
+    // left subtree.  The two halves of the top `spawn` levels are built on
+    // two threads: they touch disjoint ranks and ids.
+    void build(int l, int u, int depth, int id, int spawn, int &maxDepth) {
+        t.l[id] = l;
+        t.u[id] = u;
+        t.depth[id] = depth;
+        t.escape[id] = id + count(u - l + 1);
+        maxDepth = std::max(maxDepth, depth);
+        if (u - l <= bucket) {
+            t.leaf[id] = 1;
+            return;
         }
-        t.leaf.push_back(0);
+        t.leaf[id] = 0;
         int best = 0;
         double bsp = -1.0;
         for (int c = 0; c < 3; ++c) {
-            double sp = sampled_spread(pts, t.perm.data(), c, it.l, it.u);
+            double sp = sampled_spread(pts, t.perm.data(), c, l, u);
             if (sp > bsp) {
                 best = c;
                 bsp = sp;
             }
         }
-        int m = (it.l + it.u) / 2;
-        select_rank(pts, t.perm.data(), best, m, it.l, it.u);
-        work.push_back({m + 1, it.u, it.depth + 1, id});  // right: id recorded when popped
-        work.push_back({it.l, m, it.depth + 1, -1});      // left child gets id+1
-    }
-    const int nn = t.nodes();
-    for (int k = nn - 1; k >= 0; --k) t.escape[k] = t.leaf[k] ? k + 1 : t.escape[rightChild[k]];
-    // setCenters: unweighted centroid of the range, 1/max distance
-    t.X.assign(3 * nn, 0.0);
-    t.oradius.assign(nn, 0.0);
-    for (int k = 0; k < nn; ++k) {
-        double s[3] = {0, 0, 0};
-        for (int i = t.l[k]; i <= t.u[k]; ++i)
-            for (int c = 0; c < 3; ++c) s[c] += pts[3 * t.perm[i] + c];
-        const int cnt = t.u[k] - t.l[k] + 1;
-        for (int c = 0; c < 3; ++c) s[c] = s[c] / cnt;
-        double radius = 0;
-        for (int i = t.l[k]; i <= t.u[k]; ++i) {
-            double dx = pts[3 * t.perm[i]] - s[0], dy = pts[3 * t.perm[i] + 1] - s[1],
-                   dz = pts[3 * t.perm[i] + 2] - s[2];
-            radius = std::max(radius, std::sqrt(dx * dx + dy * dy + dz * dz));
+        const int m = (l + u) / 2;
+        select_rank(pts, t.perm.data(), best, m, l, u);
+        const int leftId = id + 1, rightId = id + 1 + count(m - l + 1);
+        if (spawn > 0) {
+            int rightDepth = 0;
+            std::thread right([&] { build(m + 1, u, depth + 1, rightId, spawn - 1, rightDepth); });
+            build(l, m, depth + 1, leftId, spawn - 1, maxDepth);
+            right.join();
+            maxDepth = std::max(maxDepth, rightDepth);
+        } else {
+            build(l, m, depth + 1, leftId, 0, maxDepth);
+            build(m + 1, u, depth + 1, rightId, 0, maxDepth);
         }
-        for (int c = 0; c < 3; ++c) t.X[3 * k + c] = s[c];
-        t.oradius[k] = 1.0 / radius;
     }
+};
+
+}  // namespace
+
+void build_kdtree(const double *pts, int n, int bucket, FlatTree &t) {
+    t = FlatTree();
+    t.n = n;
+    t.bucket = bucket;
+    if (n <= 0) return;
+    t.perm.resize(n);
+    for (int i = 0; i < n; ++i) t.perm[i] = i;
+    std::map<int, int> memo;
+    const int nn = subtree_nodes(n, bucket, memo);
+    t.l.assign(nn, 0);
+    t.u.assign(nn, 0);
+    t.depth.assign(nn, 0);
+    t.escape.assign(nn, 0);
+    t.leaf.assign(nn, 0);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    int spawn = 0;  // 2^spawn threads in the top levels
+    while ((2u << spawn) <= std::min(hw, 16u) && spawn < 4) ++spawn;
+    KdBuild kb{pts, bucket, t, memo};
+    int maxDepth = 1;
+    kb.build(0, n - 1, 1, 0, n > 4096 ? spawn : 0, maxDepth);
+    t.maxDepth = maxDepth;
+    // setCenters: unweighted centroid of the range, 1/max distance (one
+    // node's work is independent of every other's)
+    t.X.assign(3 * size_t(nn), 0.0);
+    t.oradius.assign(nn, 0.0);
+    auto centres = [&](int k0, int k1) {
+        for (int k = k0; k < k1; ++k) {
+            double s[3] = {0, 0, 0};
+            for (int i = t.l[k]; i <= t.u[k]; ++i)
+                for (int c = 0; c < 3; ++c) s[c] += pts[3 * t.perm[i] + c];
+            const int cnt = t.u[k] - t.l[k] + 1;
+            for (int c = 0; c < 3; ++c) s[c] = s[c] / cnt;
+            double radius = 0;
+            for (int i = t.l[k]; i <= t.u[k]; ++i) {
+                double dx = pts[3 * t.perm[i]] - s[0], dy = pts[3 * t.perm[i] + 1] - s[1],
+                       dz = pts[3 * t.perm[i] + 2] - s[2];
+                radius = std::max(radius, std::sqrt(dx * dx + dy * dy + dz * dz));
+            }
+            for (int c = 0; c < 3; ++c) t.X[3 * k + c] = s[c];
+            t.oradius[k] = 1.0 / radius;
+        }
+    };
+    const int nt = (n > 4096) ? int(std::min(hw, 16u)) : 1;
+    std::vector<std::thread> pool;
+    for (int q = 1; q < nt; ++q) pool.emplace_back(centres, int(int64_t(nn) * q / nt), int(int64_t(nn) * (q + 1) / nt));
+    centres(0, int(int64_t(nn) / nt));
+    for (auto &th : pool) th.join();
 }
 
 }  // namespace idw
