@@ -61,3 +61,29 @@ def build_gpu(m, opts=None, sym=True, precision="fp64"):
         mesh.createCommonGrid(m["xv0"])
         mesh.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
     return mesh
+
+
+def open_cylinder(n_around=24, n_along=8, radius=1.0, length=3.0, n_vol=3000, seed=3):
+    """An open tube (radius, axis z, no end caps) of quads and seeded volume
+    points around it.  Every surface normal is perpendicular to z, so a
+    rotation about z is what each node's Rodrigues rotation reproduces."""
+    th = np.linspace(0.0, 2 * np.pi, n_around, endpoint=False)
+    z = np.linspace(0.0, length, n_along + 1)
+    pts = np.array([[radius * np.cos(t), radius * np.sin(t), zz] for zz in z for t in th])
+    conn = []
+    for j in range(n_along):
+        for i in range(n_around):
+            a = j * n_around + i
+            b = j * n_around + (i + 1) % n_around
+            conn += [a, b, b + n_around, a + n_around]
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(1.2, 6.0, n_vol)
+    t = rng.uniform(0.0, 2 * np.pi, n_vol)
+    xv0 = np.stack([r * np.cos(t), r * np.sin(t), rng.uniform(-1.0, length + 1.0, n_vol)], axis=1)
+    return {"pts": pts, "conn": np.array(conn, dtype=np.int32), "faceSizes": np.full(n_along * n_around, 4, np.int32),
+            "xv0": xv0}
+
+
+def rotation_z(deg):
+    c, s = np.cos(np.radians(deg)), np.sin(np.radians(deg))
+    return np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])

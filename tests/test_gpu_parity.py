@@ -122,6 +122,23 @@ def test_warp_deriv_batch_matches_single(wing, built_lib):
         np.testing.assert_allclose(batch[s], single, rtol=1e-12, atol=1e-12 * np.abs(single).max())
 
 
+@pytest.mark.parametrize("precision,mode", [("fp64", "fast"), ("fp64", "exact"), ("mixed", "fast"),
+                                            ("mixed", "exact")])
+def test_rigid_rotation_gpu(precision, mode, built_lib):
+    # an open tube turned about its axis: every node has M_i = R, b_i = 0, so
+    # the volume turns by R (the mixed form carries R - I in its reference
+    # motion, leaving nothing to round in FP32)
+    from tests.meshes import open_cylinder, rotation_z
+
+    m = open_cylinder()
+    R = rotation_z(10.0)
+    g = build_gpu(m, {"evalMode": mode}, sym=False, precision=precision)
+    g.setSurfaceCoordinates(m["pts"] @ R.T)
+    g.warpMesh()
+    tol = 1e-12 if precision == "fp64" else 1e-10
+    np.testing.assert_allclose(g.getWarpGrid().reshape(-1, 3), m["xv0"] @ R.T, rtol=0, atol=tol)
+
+
 def test_rigid_translation_gpu(sphere, built_lib):
     g = build_gpu(sphere, precision="fp64")
     t = np.array([0.25, 0.5, -0.125])

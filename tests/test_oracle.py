@@ -50,6 +50,21 @@ def test_rigid_translation(sphere, mode, oracle_lib):
     np.testing.assert_allclose(xv - sphere["xv0"], np.broadcast_to(t, xv.shape), atol=1e-13)
 
 
+@pytest.mark.parametrize("mode", ["fast", "exact"])
+def test_rigid_rotation_about_the_normals_plane(mode, oracle_lib):
+    # every normal of an open tube is perpendicular to its axis: turning the
+    # tube about the axis gives every node M_i = R and b_i = 0, so the warped
+    # volume is the same rotation of the initial one
+    from tests.meshes import open_cylinder, rotation_z
+
+    m = open_cylinder()
+    R = rotation_z(10.0)
+    om = build_oracle(m, {"evalMode": mode}, sym=False)
+    om.set_surface_coordinates(m["pts"] @ R.T)
+    xv = om.warp()
+    np.testing.assert_allclose(xv, m["xv0"] @ R.T, rtol=0, atol=1e-12)
+
+
 def test_identity_surface_gives_identity_volume(sphere, oracle_lib):
     om = build_oracle(sphere)
     om.set_surface_coordinates(sphere["pts"])
