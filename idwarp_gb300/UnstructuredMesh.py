@@ -157,11 +157,13 @@ class USMesh(BaseSolver):
             )
         if isinstance(coordinates, np.ndarray) or not hasattr(coordinates, "data_ptr"):
             coordinates = np.ascontiguousarray(coordinates, dtype=np.float64)
-            if not np.all(np.isfinite(coordinates)):
-                raise Error("Non-finite surface coordinates supplied to setSurfaceCoordinates.")
         ptr, where = _lib.vptr(coordinates)
-        self._chk(self.lib.idw_set_surface_coordinates(self.ctx, ptr, 3 * self.nSurf, where),
-                    "setSurfaceCoordinates")
+        # host arrays are checked for non-finite values by the library, which
+        # then leaves the surface unchanged
+        rc = self.lib.idw_set_surface_coordinates(self.ctx, ptr, 3 * self.nSurf, where)
+        if rc == _lib.IDW_ERR_NONFINITE:
+            raise Error("Non-finite surface coordinates supplied to setSurfaceCoordinates.")
+        self._chk(rc, "setSurfaceCoordinates")
         self._surfVersion += 1
 
     def setExternalMeshIndices(self, ind):

@@ -113,3 +113,29 @@ def test_synthetic_sizes():
     assert np.all(w["xv0"][:, 1] >= -1e-12)
     xs = S.wing_perturbation(w["pts"], seed=2)
     assert np.isfinite(xs).all() and np.abs(xs - w["pts"]).max() < 0.3
+
+
+def test_nonfinite_surface_coordinates_raise_error():
+    # the library's non-finite status becomes the reference's Error, and the
+    # call never counts as a new surface
+    import math
+
+    from idwarp_gb300 import Error, USMesh
+    from idwarp_gb300 import _lib
+
+    class FakeLib:
+        def idw_set_surface_coordinates(self, ctx, ptr, n, where):
+            import ctypes as C
+
+            a = (C.c_double * n).from_address(ptr.value)
+            return _lib.IDW_ERR_NONFINITE if any(not math.isfinite(v) for v in a) else 0
+
+    m = USMesh.__new__(USMesh)
+    m.nSurf, m.ctx, m.lib, m._surfVersion = 4, None, FakeLib(), 0
+    m.setSurfaceCoordinates(np.ones((4, 3)))
+    assert m._surfVersion == 1
+    bad = np.ones((4, 3))
+    bad[2, 1] = np.inf
+    with pytest.raises(Error, match="Non-finite"):
+        m.setSurfaceCoordinates(bad)
+    assert m._surfVersion == 1
