@@ -7,6 +7,7 @@ evaluation runs in hand-written sm_103a CUDA kernels behind the C ABI of
 from .options import Error
 from .UnstructuredMesh import USMesh, pointReduce
 from .MultiUnstructuredMesh import MultiUSMesh
+from .complex_step import MultiUSMesh_C, USMesh_C
 
 __version__ = "0.1.0"
-__all__ = ["USMesh", "MultiUSMesh", "Error", "pointReduce"]
+__all__ = ["USMesh", "MultiUSMesh", "USMesh_C", "MultiUSMesh_C", "Error", "pointReduce"]

@@ -139,3 +139,12 @@ def test_nonfinite_surface_coordinates_raise_error():
     with pytest.raises(Error, match="Non-finite"):
         m.setSurfaceCoordinates(bad)
     assert m._surfVersion == 1
+
+
+def test_complex_step_classes_raise_a_clear_error():
+    # importable like the reference's, but the complex build is not on the GPU path
+    from idwarp_gb300 import Error, MultiUSMesh_C, USMesh_C
+
+    for cls in (USMesh_C, MultiUSMesh_C):
+        with pytest.raises(Error, match="warpDeriv"):
+            cls(options={})
