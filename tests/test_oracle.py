@@ -187,3 +187,18 @@ def test_tree_invariants(wing, oracle_lib):
     surf = om.surface()
     csum = np.concatenate([[0.0], np.cumsum(surf["Ai"])])
     np.testing.assert_allclose(t["Ai"], csum[t["u"] + 1] - csum[t["l"]], rtol=1e-12)
+
+
+def test_dry_run_costs_closed_form_at_errtol_zero(oracle_lib):
+    # kd_tree.F90:789-830 with errTol 0: no approximation is accepted, so each
+    # mirror walk visits every interior node (0.5) and every point (1), and the
+    # cost of a node is nLoop (0.5 nInterior + n) / n
+    from tests.meshes import wing_small
+
+    m = wing_small()
+    om = build_oracle(m, {"errTol": 0.0})
+    t = om.tree()
+    n = om.sizes()["nUnique"]
+    nloop = om.sizes()["nLoop"]
+    want = nloop * (0.5 * int(np.sum(t["dnum"] != 0)) + n) / n
+    np.testing.assert_allclose(om.dry_run(), want, rtol=1e-14)
