@@ -156,40 +156,149 @@ def fp32_peak_tflops():
     return best if best > 0 else None
 
 
-def run_cpu_baseline(m, budget_s=15.0, threads=None, seed=0):
-    """Oracle (CPU restatement of the reference) warp over a seeded sample of volume nodes."""
-    from oracle.pyoracle import OracleMesh, max_threads, set_threads
+def cpu_info():
+    """CPU model and core counts of this host, recorded beside the CPU numbers."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for ln in f:
+                    if ln.lower().startswith(("model name", "cpu part")):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except Exception:
+            pass
+    try:
+        usable = len(os.sched_getaffinity(0))
+    except Exception:
+        usable = os.cpu_count()
+    return {"cpu_model": model, "nproc": os.cpu_count(), "usable_cores": usable, "machine": os.uname().machine}
 
-    if threads:
-        set_threads(threads)
-    nthr = max_threads()
+
+def workload_config(cfg, m, mode, nunique, world):
+    """The `config` object of both arms' JSON lines (the same dict, so the two
+    lines name the same workload)."""
+    nvol = len(m["xv0"])
+    return {"workload": "wing_shell_%dx%dx%d" % CONFIGS[cfg], "volume_nodes": nvol, "surface_points": len(m["pts"]),
+            "unique_surface_nodes": int(nunique), "errTol": ERR_TOL, "mode": mode,
+            "symmetry_planes": len(m["symmetryPlanes"]), "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs %s L2 (Xv0+Xv+den0+den ~%.0f MB per step)" % (
+                "larger than" if nvol * 64 > 129e6 else "fit in", nvol * 64 / 1e6)}
+
+
+class OracleSample:
+    """The oracle (CPU restatement of the reference) set up on a seeded sample
+    of the workload's volume nodes: the volume nodes are independent given
+    the surface, so a sample is a bounded piece of the same work."""
+
+    def __init__(self, m, idx, library=None, mode="fast"):
+        from oracle.pyoracle import OracleMesh
+
+        o = dict(mesh_options(m, "fp64", mode))
+        self.idx = idx
+        self.om = OracleMesh({k: o[k] for k in ("aExp", "bExp", "LdefFact", "alpha", "errTol", "evalMode",
+                                                "bucketSize")}, library=library)
+        self.om.set_volume(m["xv0"][idx])
+        planes = m["symmetryPlanes"]
+        self.om.set_symmetry(np.array([p[0] for p in planes]).reshape(-1, 3),
+                             np.array([p[1] for p in planes]).reshape(-1, 3))
+        self.om.set_surface_definition(m["pts"], m["conn"], m["faceSizes"])
+        self.xs = m["xs"]
+
+    def step(self):
+        """One step of the CPU path: surface coordinates in, the sample warped."""
+        self.om.set_surface_coordinates(self.xs)
+        return self.om.warp()
+
+
+def run_cpu_baseline(m, budget_s=10.0, seed=0):
+    """The oracle's timing build (-O3, tuned for this CPU, OpenMP on every
+    usable core) warping a seeded sample of the workload's volume nodes sized
+    to about budget_s, plus the same on one core over a smaller sample.
+    Returns the JSON object and the sample (indices, warped nodes) that the
+    parity check reuses with the checker build."""
+    from oracle.build import timing_flags
+    from oracle.pyoracle import max_threads, set_threads, timing_library
+
+    L = timing_library()
+    nthr = max_threads(L)
     rng = np.random.default_rng(seed)
     nvol = len(m["xv0"])
-    # calibrate on a 20k-node sample (after one run that starts the thread
-    # pool), then size the sample to ~budget_s of warp time
-    n = min(nvol, 20000)
-    result = None
-    for attempt in range(3):
-        idx = np.sort(rng.choice(nvol, n, replace=False))
-        o = dict(mesh_options(m, "fp64"))
-        om = OracleMesh({k: o[k] for k in ("aExp", "bExp", "LdefFact", "alpha", "errTol", "evalMode", "bucketSize")})
-        om.set_volume(m["xv0"][idx])
-        planes = m["symmetryPlanes"]
-        om.set_symmetry(np.array([p[0] for p in planes]), np.array([p[1] for p in planes]))
-        om.set_surface_definition(m["pts"], m["conn"], m["faceSizes"])
-        om.set_surface_coordinates(m["xs"])
-        t0 = time.perf_counter()
-        om.warp()
-        dt = time.perf_counter() - t0
-        result = (n, dt)
-        if attempt == 2 or n == nvol:
-            break
-        if attempt == 1:
-            n = int(max(20000, min(nvol, n * budget_s / max(dt, 1e-3))))
-    n, dt = result
-    return {"value": n / dt, "unit": "volume nodes/s", "cores": nthr, "kind": "port",
-            "sample": "%d of %d volume nodes (seeded uniform sample), fast mode errTol %g, FP64, %.2f s" % (
-                n, nvol, ERR_TOL, dt)}
+    # calibrate on 20k nodes (after one run that starts the thread pool)
+    idx = np.sort(rng.choice(nvol, min(nvol, 20000), replace=False))
+    s = OracleSample(m, idx, L)
+    s.step()
+    t0 = time.perf_counter()
+    s.step()
+    rate = len(idx) / (time.perf_counter() - t0)
+    n = int(min(nvol, max(20000, rate * budget_s)))
+    idx = np.sort(rng.choice(nvol, n, replace=False))
+    s = OracleSample(m, idx, L)
+    t0 = time.perf_counter()
+    xv = s.step()
+    dt = time.perf_counter() - t0
+    # one core, about budget_s / 3 of work
+    n1 = int(min(n, max(2000, rate / max(nthr, 1) * budget_s / 3)))
+    s1 = OracleSample(m, idx[:n1], L)
+    set_threads(1, L)
+    t0 = time.perf_counter()
+    s1.step()
+    dt1 = time.perf_counter() - t0
+    set_threads(nthr, L)
+    del s1
+    line = {"value": n / dt, "unit": "volume nodes/s", "cores": nthr, "kind": "port",
+            "sample": "%d of %d volume nodes (seeded uniform sample), fast mode errTol %g, FP64, %.2f s per step "
+                      "(setSurfaceCoordinates + warpMesh)" % (n, nvol, ERR_TOL, dt),
+            "value_1core": n1 / dt1, "sample_1core": "%d nodes, %.2f s" % (n1, dt1),
+            "build": "oracle/idw_oracle.cpp timing build: g++ " + timing_flags()}
+    line.update(cpu_info())
+    return line, idx, xv
+
+
+def run_parity(m, idx, xv_timing, grids, gpu_stats_fn):
+    """The GPU path against the oracle at this workload: the oracle's checker
+    build (no FMA contraction) warps the sampled volume nodes; the GPU grids
+    of the whole mesh are compared at the same nodes, and GPU meshes of just
+    the sampled nodes give the GPU's decision counts for the same nodes.
+    The timing build's difference from the checker is the case's rounding
+    sensitivity (different rounding order of the same formulas)."""
+    s = OracleSample(m, idx)
+    xo = s.step()
+    ost = s.om.stats()
+    L = s.om.ldef0()
+    out = {"n_nodes": int(len(idx)), "sample": "the CPU baseline's sample", "Ldef": L,
+           "oracle": {"leafPairs": ost["leafPairs"], "approx": ost["approx"]},
+           "rounding_sensitivity_over_Ldef": float(np.abs(xv_timing - xo).max() / L)}
+    del s
+    sens = out["rounding_sensitivity_over_Ldef"]
+    ok = True
+    for prec, bar in (("mixed", 1e-8), ("fp64", 1e-12)):
+        st = gpu_stats_fn(prec, idx)
+        res = {"leafPairs": st["leafPairs"], "approx": st["approx"],
+               "leafPairs_equal": st["leafPairs"] == ost["leafPairs"], "approx_equal": st["approx"] == ost["approx"],
+               "bar_over_Ldef": max(bar, 4 * sens)}
+        e = np.abs(st["xv"] - xo).max(axis=1) / L
+        res["sample_mesh_max_err_over_Ldef"] = float(e.max())
+        res["sample_mesh_rms_err_over_Ldef"] = float(np.sqrt(np.mean(e ** 2)))
+        g = grids.get(prec)
+        if g is not None:
+            e = np.abs(g[idx] - xo).max(axis=1) / L
+            res["max_err_over_Ldef"] = float(e.max())
+            res["rms_err_over_Ldef"] = float(np.sqrt(np.mean(e ** 2)))
+        worst = max(res["sample_mesh_max_err_over_Ldef"], res.get("max_err_over_Ldef", 0.0))
+        res["pass"] = bool(res["leafPairs_equal"] and res["approx_equal"] and worst <= res["bar_over_Ldef"])
+        ok = ok and res["pass"]
+        out[prec] = res
+    out["pass"] = ok
+    return out
 
 
 def replica_throughput(ms_step, units_per_rank, world, device):
@@ -438,20 +547,44 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
+        from oracle.build import timing_flags
+        from oracle.pyoracle import max_threads, timing_library
+
         m = make_workload(args.config)
+        L = timing_library()
+        nthr = max_threads(L)
+        nvol = len(m["xv0"])
+        rng = np.random.default_rng(100)
+        # one step = setSurfaceCoordinates + warpMesh over a seeded sample of
+        # the workload's volume nodes, sized to about 1.5 s on every core
+        idx = np.sort(rng.choice(nvol, min(nvol, 20000), replace=False))
+        cal = OracleSample(m, idx, L)
+        cal.step()
+        t0 = time.perf_counter()
+        cal.step()
+        rate = len(idx) / (time.perf_counter() - t0)
+        nunique = cal.om.sizes()["nUnique"]
+        del cal
+        n = int(min(nvol, max(20000, 1.5 * rate)))
+        smp = OracleSample(m, np.sort(rng.choice(nvol, n, replace=False)), L)
         per_step = []
-        info = None
-        for s in range(args.warmup + args.steps):
-            info = run_cpu_baseline(m, budget_s=4.0, seed=100 + s)
-            if s >= args.warmup:
-                per_step.append(info["value"])
+        for st in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            smp.step()
+            dt = time.perf_counter() - t0
+            if st >= args.warmup:
+                per_step.append(n / dt)
         v = float(np.median(per_step))
+        cpu = {"value": v, "unit": unit, "cores": nthr, "kind": "port",
+               "sample": "%d of %d volume nodes (seeded uniform sample) per step, fast mode errTol %g, FP64; "
+                         "median of %d steps" % (n, nvol, ERR_TOL, args.steps),
+               "build": "oracle/idw_oracle.cpp timing build: g++ " + timing_flags()}
+        cpu.update(cpu_info())
         line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": "wing_shell_%dx%dx%d" % CONFIGS[args.config],
-                                                "errTol": ERR_TOL, "mode": "fast"},
-                "cpu_baseline": {"value": v, "unit": unit, "cores": info["cores"], "kind": "port",
-                                 "sample": info["sample"]},
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(args.config, m, args.mode, nunique, world),
+                "cpu_baseline": cpu,
                 "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "CPU restatement of the reference algorithm (oracle/idw_oracle.cpp); the Fortran/PETSc "
                         "reference cannot be built on this image"}
@@ -486,7 +619,9 @@ def main():
     xs_ptr = C.c_void_p(xs_dev.data_ptr())
 
     def step():
-        L.idw_set_surface_coordinates(mesh.ctx, xs_ptr, 3 * npts, _lib.IDW_DEVICE)
+        rc = L.idw_set_surface_coordinates(mesh.ctx, xs_ptr, 3 * npts, _lib.IDW_DEVICE)
+        if rc != 0:
+            _lib.check(L, mesh.ctx, rc, "setSurfaceCoordinates")
         rc = L.idw_warp_mesh(mesh.ctx)
         if rc != 0:
             _lib.check(L, mesh.ctx, rc, "warpMesh")
@@ -533,10 +668,7 @@ def main():
         "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "wing_shell_%dx%dx%d" % CONFIGS[args.config], "volume_nodes": nvol,
-                   "surface_points": npts, "unique_surface_nodes": st["nUnique"], "errTol": ERR_TOL,
-                   "mode": args.mode, "symmetry_planes": 1, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (Xv0+Xv+den0+den ~%.0f MB per step)" % (nvol * 64 / 1e6)},
+        "config": workload_config(args.config, m, args.mode, st["nUnique"], world),
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": int(xs_host.nbytes),
                 "d2h_bytes_per_step": int(grid.nbytes)},
         "clocks": clk,
@@ -553,8 +685,8 @@ def main():
     achieved = flops / (kernel_ms * 1e-3) / 1e12 if kernel_ms > 0 else None
     # DRAM traffic of the walk: ncu dram__bytes_read.sum + dram__bytes_write.sum of
     # k_walk_mixed on the 2M-node wing (148.4 + 42.0 MB for 2,025,050 volume
-    # nodes, profiles/k_walk_mixed_wing2M_full.md), scaled by volume nodes: the
-    # traffic is the per-node records and accumulators, the tree stays in L2
+    # nodes), scaled by volume nodes: the traffic is the per-node records and
+    # accumulators, the tree stays in L2
     traffic = 94.0 * nvol
     walk_kernel = "k_exact_mixed" if args.mode == "exact" else "k_walk_mixed"
     out["roofline"] = {"bound": "fp32", "kernel": walk_kernel, "achieved": achieved, "unit": "TFLOP/s",
@@ -701,7 +833,24 @@ def main():
             del mr
 
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = run_cpu_baseline(m)
+        out["cpu_baseline"], idx, xv_cpu = run_cpu_baseline(m)
+        # parity at this workload: the oracle's checker build on the same sample
+        grids = {"mixed": grid.reshape(-1, 3)}
+        if not args.no_extras:
+            grids["fp64"] = x64
+
+        def sample_run(prec, idx):
+            ms = dict(m)
+            ms["xv0"] = m["xv0"][idx]
+            g = build_mesh(ms, prec)
+            g.setSurfaceCoordinates(m["xs"])
+            g.warpMesh()
+            r = g.getStats()
+            r["xv"] = g.getWarpGrid().reshape(-1, 3)
+            del g
+            return r
+
+        out["parity"] = run_parity(m, idx, xv_cpu, grids, sample_run)
     if rank == 0:
         print(json.dumps(out))
     if dist_on:

@@ -600,7 +600,11 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CK(cudaMemcpyAsync(c->nodeAi.p, nodeAi.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, st));
     // error tables (kd_tree.F90:1528-1544) with the creation-time law
     WeightLaw law0 = make_init_law(c);
-    launch_compute_errors(tree_dev(c), c->ptXA.p, law0, c->nodeErr.p, nullptr, 0, st);
+    {
+        const int rc = launch_compute_errors(tree_dev(c), c->ptXA.p, law0, c->nodeErr.p, st);
+        if (rc == -2) return fail(c, IDW_ERR_NOMEM, "computeErrors: scratch allocation failed");
+        if (rc) return fail(c, IDW_ERR_CUDA, "computeErrors: %s", cudaGetErrorString(cudaGetLastError()));
+    }
     e = check_launch(c, "computeErrors");
     if (e) return e;
     // FP32 companions: node records (split centroid, radius, area, error

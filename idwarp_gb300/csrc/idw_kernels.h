@@ -140,8 +140,8 @@ void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, co
                     cudaStream_t st);
 
 // Set-up kernels (idw_setup.cu)
-void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err,
-                           double *scratch, int64_t scratchLen, cudaStream_t st);
+// Returns 0, -1 on a CUDA error, -2 when its scratch cannot be allocated.
+int launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err, cudaStream_t st);
 void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
                          const SymPlanes &sym, double *den0, cudaStream_t st);
 // estimate of the common-order nodes 0, stride, 2 stride, ... into out; returns their count

@@ -6,6 +6,7 @@
 //   dryRun         src/modules/kd_tree.F90:789-830, driven by src/warp/initializeWarping.F90:258-266
 #include <cub/cub.cuh>
 
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -376,14 +377,12 @@ inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 }  // namespace
 
 
-void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err,
-                           double *scratch, int64_t scratchLen, cudaStream_t st) {
-    (void)scratch;
-    (void)scratchLen;
+int launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err, cudaStream_t st) {
     // Build the (node, chunk) work list on the host.
     std::vector<int4> info(t.nNodes);
-    cudaMemcpyAsync(info.data(), t.info, sizeof(int4) * t.nNodes, cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
+    if (cudaMemcpyAsync(info.data(), t.info, sizeof(int4) * t.nNodes, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return -1;
     std::vector<ErrItem> items;
     std::vector<int> item0, interior;
     for (int q = 0; q < t.nNodes; ++q) {
@@ -393,25 +392,37 @@ void launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &
         for (int a = info[q].x; a <= info[q].y; a += kErrChunk) items.push_back({q, a, min(a + kErrChunk, info[q].y + 1), 0});
     }
     item0.push_back(int(items.size()));
-    cudaMemsetAsync(err, 0, sizeof(double) * kNerr * t.nNodes, st);
-    if (interior.empty()) return;
-    ErrItem *dItems;
-    int *dItem0, *dInterior;
-    double *dPart;
-    cudaMalloc(&dItems, sizeof(ErrItem) * items.size());
-    cudaMalloc(&dItem0, sizeof(int) * item0.size());
-    cudaMalloc(&dInterior, sizeof(int) * interior.size());
-    cudaMalloc(&dPart, sizeof(double) * 240 * items.size());
-    cudaMemcpyAsync(dItems, items.data(), sizeof(ErrItem) * items.size(), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dItem0, item0.data(), sizeof(int) * item0.size(), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(dInterior, interior.data(), sizeof(int) * interior.size(), cudaMemcpyHostToDevice, st);
-    k_err_partial<<<int(items.size()), 256, 0, st>>>(t, ptXA, law, dItems, dPart);
-    k_err_final<<<int(interior.size()), 256, 0, st>>>(t, law, dItem0, dInterior, dPart, err);
-    cudaStreamSynchronize(st);
-    cudaFree(dItems);
-    cudaFree(dItem0);
-    cudaFree(dInterior);
-    cudaFree(dPart);
+    if (cudaMemsetAsync(err, 0, sizeof(double) * kNerr * t.nNodes, st) != cudaSuccess) return -1;
+    if (interior.empty()) return 0;
+    ErrItem *dItems = nullptr;
+    int *dItem0 = nullptr, *dInterior = nullptr;
+    double *dPart = nullptr;
+    // every allocation checked before any copy or launch uses it
+    int rc = 0;
+    if (cudaMalloc(&dItems, sizeof(ErrItem) * items.size()) != cudaSuccess ||
+        cudaMalloc(&dItem0, sizeof(int) * item0.size()) != cudaSuccess ||
+        cudaMalloc(&dInterior, sizeof(int) * interior.size()) != cudaSuccess ||
+        cudaMalloc(&dPart, sizeof(double) * 240 * items.size()) != cudaSuccess) {
+        rc = -2;
+    } else if (cudaMemcpyAsync(dItems, items.data(), sizeof(ErrItem) * items.size(), cudaMemcpyHostToDevice, st) !=
+                   cudaSuccess ||
+               cudaMemcpyAsync(dItem0, item0.data(), sizeof(int) * item0.size(), cudaMemcpyHostToDevice, st) !=
+                   cudaSuccess ||
+               cudaMemcpyAsync(dInterior, interior.data(), sizeof(int) * interior.size(), cudaMemcpyHostToDevice,
+                               st) != cudaSuccess) {
+        rc = -1;
+    } else {
+        k_err_partial<<<int(items.size()), 256, 0, st>>>(t, ptXA, law, dItems, dPart);
+        k_err_final<<<int(interior.size()), 256, 0, st>>>(t, law, dItem0, dInterior, dPart, err);
+        if (cudaGetLastError() != cudaSuccess) rc = -1;
+    }
+    // the scratch is freed only once the kernels that read it are done
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
+    if (dItems) cudaFree(dItems);
+    if (dItem0) cudaFree(dItem0);
+    if (dInterior) cudaFree(dInterior);
+    if (dPart) cudaFree(dPart);
+    return rc;
 }
 
 void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
@@ -482,14 +493,20 @@ void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *pt
 // k-th node in Morton order.
 int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
                 cudaStream_t st) {
+    // cub takes the item count as int
+    if (nVol > INT_MAX) return -1;
     size_t tmp = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tmp, codes, codesAlt, idx, perm, (int)nVol, 0, 63, st);
+    if (cub::DeviceRadixSort::SortPairs(nullptr, tmp, codes, codesAlt, idx, perm, int(nVol), 0, 63, st) !=
+        cudaSuccess)
+        return -1;
     void *dTmp = nullptr;
     if (cudaMalloc(&dTmp, tmp) != cudaSuccess) return -1;
-    cub::DeviceRadixSort::SortPairs(dTmp, tmp, codes, codesAlt, idx, perm, (int)nVol, 0, 63, st);
-    cudaStreamSynchronize(st);
+    int rc = 0;
+    if (cub::DeviceRadixSort::SortPairs(dTmp, tmp, codes, codesAlt, idx, perm, int(nVol), 0, 63, st) != cudaSuccess)
+        rc = -1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
     cudaFree(dTmp);
-    return 0;
+    return rc;
 }
 
 }  // namespace idw

@@ -213,7 +213,10 @@ int idw_warp_deriv_fwd_batch(void *ctx, const double *dxs, int32_t ndir, double 
  * 12 doubles per unique surface node and per tree node, plus 12 per surface
  * node in mixed precision, must fit in 6*2^20 doubles (with bucketSize 8
  * about 210k unique surface nodes in mixed precision, 360k in FP64), else
- * IDW_ERR_LIMIT.  Calls that overlap in time
+ * IDW_ERR_LIMIT.  The array belongs to the library's device code, so every
+ * process that loads libidwarp_gb300.so holds those 48 MiB on each device it
+ * uses the library on, until it exits, whether or not it ever calls this
+ * entry point.  Calls that overlap in time
  * (several contexts or streams at once) race on that scratch.  The first
  * call on a device looks the scratch up (cudaGetSymbolAddress): make it
  * before any stream capture. */

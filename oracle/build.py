@@ -46,5 +46,27 @@ def build_oracle_contracted():
     return out
 
 
+def build_oracle_timing(force=False):
+    """The timing build of the same source for the CPU baseline: -O3, tuned
+    for the CPU it is built on (-mcpu=native on aarch64; built on the machine
+    that runs it), FMA contraction allowed, OpenMP.  Its results differ from
+    the checker build's by rounding only; it is never used as the checker."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    out = os.path.join(OUT_DIR, "liboracle_timing.so")
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
+        return out
+    tune = ["-mcpu=native"] if os.uname().machine == "aarch64" else []
+    subprocess.run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=fast"] + tune +
+                   [SRC, "-o", out + ".tmp"], check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def timing_flags():
+    """The compiler flags of the timing build (recorded beside its numbers)."""
+    tune = ["-mcpu=native"] if os.uname().machine == "aarch64" else []
+    return " ".join(["-O3", "-fopenmp", "-ffp-contract=fast"] + tune)
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True, verbose=True))

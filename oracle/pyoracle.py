@@ -12,6 +12,7 @@ import numpy as np
 from .build import build_oracle
 
 _lib = None
+_libs = {}
 
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
@@ -34,41 +35,57 @@ def use_library(path=None):
     return lib(path)
 
 
+def _bind(L):
+    L.orc_new.restype = C.c_void_p
+    L.orc_new.argtypes = [_DP]
+    L.orc_free.argtypes = [C.c_void_p]
+    L.orc_set_options.argtypes = [C.c_void_p, _DP]
+    L.orc_set_symmetry.argtypes = [C.c_void_p, _DP, _DP, C.c_int]
+    L.orc_set_volume.argtypes = [C.c_void_p, _DP, C.c_longlong]
+    L.orc_point_reduce.argtypes = [_DP, C.c_int, C.c_double, _DP, _IP]
+    L.orc_set_surface_definition.argtypes = [C.c_void_p, _DP, C.c_int, _IP, C.c_int, _IP, C.c_int]
+    L.orc_set_surface_coords.argtypes = [C.c_void_p, _DP]
+    L.orc_warp.argtypes = [C.c_void_p, _DP]
+    L.orc_warp_range.argtypes = [C.c_void_p, C.c_longlong, C.c_longlong]
+    L.orc_warp_complex.argtypes = [C.c_void_p, _DP, _DP, _DP, _DP]
+    L.orc_warp_deriv.argtypes = [C.c_void_p, _DP, _DP]
+    L.orc_warp_deriv_range.argtypes = [C.c_void_p, _DP, _DP, C.c_longlong, C.c_longlong]
+    L.orc_warp_deriv_fwd.argtypes = [C.c_void_p, _DP, _DP]
+    L.orc_sizes.argtypes = [C.c_void_p, _LP]
+    L.orc_ldef0.restype = C.c_double
+    L.orc_ldef0.argtypes = [C.c_void_p]
+    L.orc_get_tree.argtypes = [C.c_void_p, _IP, _DP, _DP, _DP]
+    L.orc_get_surface.argtypes = [C.c_void_p, _DP, _DP, _DP, _IP, _IP]
+    L.orc_get_den0.argtypes = [C.c_void_p, _DP]
+    L.orc_get_denom.argtypes = [C.c_void_p, _DP]
+    L.orc_get_nodal.argtypes = [C.c_void_p, _DP, _DP]
+    L.orc_stats.argtypes = [C.c_void_p, _LP]
+    L.orc_dry_run.argtypes = [C.c_void_p, _DP]
+    L.orc_set_threads.argtypes = [C.c_int]
+    L.orc_max_threads.restype = C.c_int
+    return L
+
+
 def lib(path=None):
+    """The oracle library (the checker build unless another build's path is
+    given); each build is loaded once."""
     global _lib
-    if _lib is None:
-        path = path or build_oracle()
-        L = C.CDLL(path)
-        L.orc_new.restype = C.c_void_p
-        L.orc_new.argtypes = [_DP]
-        L.orc_free.argtypes = [C.c_void_p]
-        for name in ["orc_set_options"]:
-            getattr(L, name).argtypes = [C.c_void_p, _DP]
-        L.orc_set_symmetry.argtypes = [C.c_void_p, _DP, _DP, C.c_int]
-        L.orc_set_volume.argtypes = [C.c_void_p, _DP, C.c_longlong]
-        L.orc_point_reduce.argtypes = [_DP, C.c_int, C.c_double, _DP, _IP]
-        L.orc_set_surface_definition.argtypes = [C.c_void_p, _DP, C.c_int, _IP, C.c_int, _IP, C.c_int]
-        L.orc_set_surface_coords.argtypes = [C.c_void_p, _DP]
-        L.orc_warp.argtypes = [C.c_void_p, _DP]
-        L.orc_warp_range.argtypes = [C.c_void_p, C.c_longlong, C.c_longlong]
-        L.orc_warp_complex.argtypes = [C.c_void_p, _DP, _DP, _DP, _DP]
-        L.orc_warp_deriv.argtypes = [C.c_void_p, _DP, _DP]
-        L.orc_warp_deriv_range.argtypes = [C.c_void_p, _DP, _DP, C.c_longlong, C.c_longlong]
-        L.orc_warp_deriv_fwd.argtypes = [C.c_void_p, _DP, _DP]
-        L.orc_sizes.argtypes = [C.c_void_p, _LP]
-        L.orc_ldef0.restype = C.c_double
-        L.orc_ldef0.argtypes = [C.c_void_p]
-        L.orc_get_tree.argtypes = [C.c_void_p, _IP, _DP, _DP, _DP]
-        L.orc_get_surface.argtypes = [C.c_void_p, _DP, _DP, _DP, _IP, _IP]
-        L.orc_get_den0.argtypes = [C.c_void_p, _DP]
-        L.orc_get_denom.argtypes = [C.c_void_p, _DP]
-        L.orc_get_nodal.argtypes = [C.c_void_p, _DP, _DP]
-        L.orc_stats.argtypes = [C.c_void_p, _LP]
-        L.orc_dry_run.argtypes = [C.c_void_p, _DP]
-        L.orc_set_threads.argtypes = [C.c_int]
-        L.orc_max_threads.restype = C.c_int
-        _lib = L
-    return _lib
+    if path is None and _lib is not None:
+        return _lib
+    p = os.path.abspath(path or build_oracle())
+    if p not in _libs:
+        _libs[p] = _bind(C.CDLL(p))
+    if path is None or _lib is None:
+        _lib = _libs[p]
+    return _libs[p]
+
+
+def timing_library():
+    """The timing build of the same source (-O3, tuned for the host CPU, FMA
+    contraction allowed): the CPU baseline's speed, never the checker."""
+    from .build import build_oracle_timing
+
+    return lib(build_oracle_timing())
 
 
 DEFAULT_OPTIONS = {
@@ -100,12 +117,12 @@ def pack_options(opts):
     )
 
 
-def set_threads(n):
-    lib().orc_set_threads(int(n))
+def set_threads(n, library=None):
+    (library or lib()).orc_set_threads(int(n))
 
 
-def max_threads():
-    return lib().orc_max_threads()
+def max_threads(library=None):
+    return (library or lib()).orc_max_threads()
 
 
 def point_reduce(pts, tol=1e-12):
@@ -120,8 +137,8 @@ def point_reduce(pts, tol=1e-12):
 class OracleMesh:
     """One oracle instance: the reference's USMesh state restated on the CPU."""
 
-    def __init__(self, options=None):
-        self.L = lib()
+    def __init__(self, options=None, library=None):
+        self.L = library or lib()
         self.opts = dict(DEFAULT_OPTIONS)
         self.opts.update(options or {})
         self._ov = pack_options(self.opts)

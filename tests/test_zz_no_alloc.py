@@ -16,12 +16,13 @@ def _noalloc(g, dxv, dxs):
                                         dxs.numel())
 
 
+@pytest.mark.parametrize("mode", ["fast", "exact"])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-12)])
-def test_noalloc_matches_warp_deriv(precision, tol, built_lib):
+def test_noalloc_matches_warp_deriv(precision, tol, mode, built_lib):
     import torch
 
     m = wing_small()
-    g = build_gpu(m, precision=precision)
+    g = build_gpu(m, {"evalMode": mode}, precision=precision)
     g.setSurfaceCoordinates(m["xs"])
     g.warpMesh()
     rng = np.random.default_rng(31)
@@ -44,6 +45,35 @@ def test_noalloc_matches_warp_deriv(precision, tol, built_lib):
     assert _noalloc(g, dxv, dxs) == 0
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_two_contexts_in_turn(built_lib):
+    # two meshes (two contexts) share the one static scratch; calls made one
+    # after the other, each finished before the next starts, must each give
+    # their own mesh's warpDeriv
+    import torch
+
+    from tests.meshes import sphere_small
+
+    stream = torch.cuda.current_stream()
+    cases = []
+    for m, prec in ((wing_small(), "mixed"), (sphere_small(), "fp64")):
+        g = build_gpu(m, precision=prec)
+        g.lib.idw_set_stream(g.ctx, C.c_void_p(stream.cuda_stream))
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        seed = np.random.default_rng(len(m["pts"])).normal(size=3 * len(m["xv0"]))
+        g.warpDeriv(seed, solverVec=False)
+        dxv = torch.tensor(seed, device="cuda")
+        dxs = torch.full((len(m["pts"]), 3), np.nan, dtype=torch.float64, device="cuda")
+        cases.append((g, g.getdXs(), dxv, dxs))
+    for rep in range(2):
+        for g, ref, dxv, dxs in (cases if rep == 0 else cases[::-1]):
+            dxs.fill_(np.nan)
+            assert _noalloc(g, dxv, dxs) == 0
+            torch.cuda.synchronize()
+            out = dxs.cpu().numpy()
+            assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max(), rep
 
 
 def test_noalloc_rejects_bad_arguments(built_lib):
