@@ -143,7 +143,7 @@ class USMesh(BaseSolver):
     def getSurfaceCoordinates(self):
         """Return all surface coordinates on this processor, shape (N,3)."""
         self._setInternalSurface()
-        coords = np.zeros((self.nSurf, 3), self.dtype)
+        coords = np.zeros((self.nSurf, 3), np.float64)
         self._chk(self.lib.idw_get_surface_coordinates(self.ctx, C.c_void_p(coords.ctypes.data), coords.size,
                                                          _lib.IDW_HOST), "getSurfaceCoordinates")
         return coords
@@ -269,7 +269,7 @@ class USMesh(BaseSolver):
         """Current grid in the order set by setExternalMeshIndices(), flat (3*n,)."""
         if self.solverMeshDOF is None:
             raise Error("setExternalMeshIndices() must be called before getSolverGrid().")
-        solverGrid = np.zeros(self.solverMeshDOF, self.dtype)
+        solverGrid = np.zeros(self.solverMeshDOF, np.float64)
         warpGrid = self.getWarpGrid()
         self._chk(self.lib.idw_warp_to_solver_grid(self.ctx, C.c_void_p(warpGrid.ctypes.data), warpGrid.size,
                                                      C.c_void_p(solverGrid.ctypes.data), solverGrid.size,
@@ -281,7 +281,7 @@ class USMesh(BaseSolver):
         contiguous float64 host array of that size to fill, e.g. in pinned
         memory for fast repeated reads."""
         if out is None:
-            out = np.zeros(3 * self.nVol, self.dtype)
+            out = np.zeros(3 * self.nVol, np.float64)
         elif out.dtype != np.float64 or out.size != 3 * self.nVol or not out.flags.c_contiguous:
             raise Error("getWarpGrid(out=...) needs a contiguous float64 array of %d entries." % (3 * self.nVol))
         self._chk(self.lib.idw_get_volume_coordinates(self.ctx, C.c_void_p(out.ctypes.data), out.size,
@@ -290,14 +290,14 @@ class USMesh(BaseSolver):
 
     def getCommonGrid(self):
         """Grid in the original (common) ordering, flat (3*nVol,)."""
-        out = np.zeros(3 * self.nVol, self.dtype)
+        out = np.zeros(3 * self.nVol, np.float64)
         self._chk(self.lib.idw_get_common_volume_coordinates(self.ctx, C.c_void_p(out.ctypes.data), out.size,
                                                                _lib.IDW_HOST), "getCommonGrid")
         return out
 
     def getdXs(self):
         """Result of the last warpDeriv(), shape (nSurf,3)."""
-        dXs = np.zeros((self.nSurf, 3), self.dtype)
+        dXs = np.zeros((self.nSurf, 3), np.float64)
         self._chk(self.lib.idw_get_dxs(self.ctx, C.c_void_p(dXs.ctypes.data), dXs.size, _lib.IDW_HOST), "getdXs")
         return dXs
 
@@ -331,7 +331,7 @@ class USMesh(BaseSolver):
         dXs = np.ascontiguousarray(np.asarray(dXs, dtype=np.float64).ravel())
         if dXs.size != 3 * self.nSurf:
             raise Error("dXs has %d entries, expected %d" % (dXs.size, 3 * self.nSurf))
-        dXvWarp = np.zeros(3 * self.nVol, self.dtype)
+        dXvWarp = np.zeros(3 * self.nVol, np.float64)
         self.warpMesh()
         self._chk(self.lib.idw_warp_deriv_fwd(self.ctx, C.c_void_p(dXs.ctypes.data), dXs.size,
                                               C.c_void_p(dXvWarp.ctypes.data), dXvWarp.size, _lib.IDW_HOST),
@@ -339,7 +339,7 @@ class USMesh(BaseSolver):
         if solverVec:
             if self.solverMeshDOF is None:
                 raise Error("setExternalMeshIndices() must be called before warpDerivFwd(solverVec=True).")
-            dXv = np.zeros(self.solverMeshDOF, self.dtype)
+            dXv = np.zeros(self.solverMeshDOF, np.float64)
             self._chk(self.lib.idw_warp_to_solver_grid(self.ctx, C.c_void_p(dXvWarp.ctypes.data), dXvWarp.size,
                                                        C.c_void_p(dXv.ctypes.data), dXv.size, _lib.IDW_HOST),
                       "warp_to_solver_grid")
@@ -496,7 +496,7 @@ class USMesh(BaseSolver):
     # ------------------------------------------------------------------
     def _solverToWarp(self, dXv):
         dXv = np.ascontiguousarray(dXv, dtype=np.float64).ravel()
-        dXvWarp = np.zeros(3 * self.nVol, self.dtype)
+        dXvWarp = np.zeros(3 * self.nVol, np.float64)
         self._chk(self.lib.idw_solver_to_warp_grid(self.ctx, C.c_void_p(dXv.ctypes.data), dXv.size,
                                                      C.c_void_p(dXvWarp.ctypes.data), dXvWarp.size, _lib.IDW_HOST),
                     "solver_to_warp_grid")

@@ -88,6 +88,9 @@ _SIGS = {
     "idw_set_surface_coordinates": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_surface_coordinates": [_VP, _VP, C.c_int64, C.c_int],
     "idw_warp_mesh": [_VP],
+    "idw_set_surface_coordinates_cs": [_VP, _VP, C.c_int64, C.c_int],
+    "idw_warp_mesh_cs": [_VP],
+    "idw_get_volume_coordinates_cs": [_VP, _VP, C.c_int64, C.c_int],
     "idw_warp_mesh_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_get_volume_coordinates": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_common_volume_coordinates": [_VP, _VP, C.c_int64, C.c_int],

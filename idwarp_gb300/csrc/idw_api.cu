@@ -13,6 +13,7 @@
 
 #include "idwarp_gb300.h"
 #include "idw_host.hpp"
+#include "idw_cplx.cuh"
 #include "idw_kernels.h"
 
 using namespace idw;
@@ -96,6 +97,11 @@ struct Ctx {
     // adjoint
     DevBuf<double> ptAdj, nodeAdj, xub, dxs;
     bool haveDxs = false;
+    // complex step: interleaved complex surface coordinates, the imaginary
+    // parts of the nodal properties and of the warped grid
+    DevBuf<double> xsC, ptMBim, nodeMBim, xvIm;
+    DevBuf<cplx> xuC;
+    bool haveCs = false;
     // solver ordering
     DevBuf<int> solverInd;
     int64_t nSolver = -1;
@@ -679,6 +685,7 @@ int idw_set_surface_coordinates(void *ctx, const double *coords, int64_t cdof, i
     if (rc) return rc;
     if (where != IDW_DEVICE) CK(cudaStreamSynchronize(c->stream));
     c->nodalValid = false;
+    c->haveCs = false;
     return IDW_OK;
 }
 
@@ -799,6 +806,96 @@ int idw_warp_mesh(void *ctx) {
     int rc = run_warp(c, c->xv.p, c->den.p);
     if (rc) return rc;
     c->haveWarp = true;
+    return IDW_OK;
+}
+
+int idw_set_surface_coordinates_cs(void *ctx, const double *coords, int64_t cdof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    if (cdof != 3 * int64_t(c->nPts))
+        return fail(c, IDW_ERR_ARG, "incorrect length of coordinates: expected %lld, received %lld",
+                    (long long)(3 * int64_t(c->nPts)), (long long)cdof);
+    CK(cudaSetDevice(c->device));
+    if (where != IDW_DEVICE && !all_finite(coords, 2 * size_t(cdof)))
+        return fail(c, IDW_ERR_NONFINITE, "non-finite surface coordinates");
+    CKA(c->xsC.alloc(2 * size_t(cdof)));
+    int rc = copy_in(c, c->xsC.p, coords, 2 * size_t(cdof), where);
+    if (rc) return rc;
+    DevBuf<double> im;
+    CKA(im.alloc(size_t(cdof)));
+    launch_split(cdof, c->xsC.p, c->xs.p, im.p, c->stream);
+    rc = check_launch(c, "complex coordinates");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    c->nodalValid = false;
+    c->haveCs = true;
+    return IDW_OK;
+}
+
+int idw_warp_mesh_cs(void *ctx) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (c->opt.precision != IDW_PREC_FP64) return fail(c, IDW_ERR_STATE, "the complex step runs in FP64 precision");
+    if (!c->haveCs) return fail(c, IDW_ERR_STATE, "complex surface coordinates must be set first");
+    CK(cudaSetDevice(c->device));
+    // real part: the ordinary warp of the real coordinates (also sets den)
+    int rc = run_warp(c, c->xv.p, c->den.p);
+    if (rc) return rc;
+    c->haveWarp = true;
+    // imaginary part: complex nodal properties, their cluster means, and
+    // the FP64 walk over (Im M + I, Im b) divided by the real denominator
+    const int n = c->nUnique;
+    CKA(c->xuC.alloc(3 * size_t(n)));
+    CKA(c->ptMBim.alloc(12 * size_t(n)));
+    CKA(c->nodeMBim.alloc(12 * size_t(c->nNodes)));
+    CKA(c->xvIm.alloc(3 * size_t(c->nVol)));
+    launch_nodal_cs(surf_dev(c), c->xuInd.p, c->xsC.p, c->xuC.p, c->ptXA.p, c->normals0.p, c->tmpAi.p,
+                    c->isCorner.p, c->opt.useRotations, c->ptMBim.p, c->stream);
+    launch_set_data(tree_dev(c), c->ptMBim.p, c->nodeMBim.p, setdata_scratch(c), c->stream);
+    rc = check_launch(c, "complex nodal properties");
+    if (rc) return rc;
+    EvalConsts k;
+    k.law = make_law(c);
+    k.errTol = c->opt.errTol;
+    k.sym = c->sym;
+    k.slotStats = 0;
+    k.exactSchedule = c->opt.exactSchedule;
+    k.precGate = 0.0;
+    PointsDev p;
+    p.xa = c->ptXA.p;
+    p.mb = c->ptMBim.p;
+    WalkOut o;
+    o.xv = c->xvIm.p;
+    o.counters = nullptr;
+    o.tangent = 1;
+    o.denIn = c->den.p;
+    launch_walk_fp64(tree_dev(c), p, vol_dev(c), c->nodeMBim.p, k, c->opt.evalMode == IDW_EVAL_EXACT, n, o,
+                     c->stream);
+    rc = check_launch(c, "complex walk");
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return IDW_OK;
+}
+
+int idw_get_volume_coordinates_cs(void *ctx, double *out, int64_t ndof, int where) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof != 3 * c->nVol)
+        return fail(c, IDW_ERR_ARG, "ndof mismatch: %lld vs %lld", (long long)ndof, (long long)(3 * c->nVol));
+    if (!c->haveCs || !c->xvIm.p) return fail(c, IDW_ERR_STATE, "no complex warp has been run");
+    CK(cudaSetDevice(c->device));
+    DevBuf<double> tmp;
+    double *dst = out;
+    if (where != IDW_DEVICE) {
+        CKA(tmp.alloc(2 * size_t(ndof)));
+        dst = tmp.p;
+    }
+    launch_interleave(ndof, c->xv.p, c->xvIm.p, dst, c->stream);
+    int rc = check_launch(c, "complex grid");
+    if (rc) return rc;
+    if (where != IDW_DEVICE) return copy_out(c, out, tmp.p, 2 * size_t(ndof), IDW_HOST);
+    CK(cudaStreamSynchronize(c->stream));
     return IDW_OK;
 }
 

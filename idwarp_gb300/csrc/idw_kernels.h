@@ -134,6 +134,15 @@ void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const
                     const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
                     cudaStream_t st, int faceProps = 1);
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st);
+
+// Complex-step nodal properties (idw_complex.cu): Xu from the interleaved
+// complex coordinates xsC, and the imaginary parts of (M + I, b) per node.
+struct cplx;
+void launch_nodal_cs(const SurfaceDev &s, const int *xuInd, const double *xsC, cplx *xu, const dbl4 *xa,
+                     const double *normals0, const double *Ai, const int *isCorner, int useRotations, double *ptMBim,
+                     cudaStream_t st);
+void launch_interleave(int64_t n, const double *re, const double *im, double *out, cudaStream_t st);
+void launch_split(int64_t n, const double *in, double *re, double *im, cudaStream_t st);
 // Tangent nodal properties: (Md [+ I], bd) per point, 12 doubles (M row-major, b).
 void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,
                     const double *Ai, const int *isCorner, int useRotations, int plusIdentity, double *ptMBd,

@@ -13,64 +13,11 @@
 // registers instead of replaying a tape.
 #include "idw_common.cuh"
 #include "idw_kernels.h"
+#include "idw_nodal_math.cuh"
 
 namespace idw {
 
 namespace {
-
-__device__ __forceinline__ void cross3(const double *a, const double *b, double *c) {
-    c[0] = a[1] * b[2] - a[2] * b[1];
-    c[1] = a[2] * b[0] - a[0] * b[2];
-    c[2] = a[0] * b[1] - a[1] * b[0];
-}
-
-// Area and unit normal of one polygonal face (fan of cross products of the
-// centre-relative vertex vectors).
-__device__ void element_props(const double *Xu, const int *conn, int np, double &area, double *normal) {
-    double c[3] = {0, 0, 0};
-    for (int k = 0; k < np; ++k) {
-        const double *p = Xu + 3 * conn[k];
-        c[0] += p[0];
-        c[1] += p[1];
-        c[2] += p[2];
-    }
-    c[0] /= double(np);
-    c[1] /= double(np);
-    c[2] /= double(np);
-    double nrm[3] = {0, 0, 0};
-    double a = 0;
-    const double *p0 = Xu + 3 * conn[0];
-    double rv0[3] = {p0[0] - c[0], p0[1] - c[1], p0[2] - c[2]};
-    double rvi[3] = {rv0[0], rv0[1], rv0[2]};
-    for (int k = 0; k < np; ++k) {
-        double rvj[3];
-        if (k < np - 1) {
-            const double *pj = Xu + 3 * conn[k + 1];
-            rvj[0] = pj[0] - c[0];
-            rvj[1] = pj[1] - c[1];
-            rvj[2] = pj[2] - c[2];
-        } else {
-            rvj[0] = rv0[0];
-            rvj[1] = rv0[1];
-            rvj[2] = rv0[2];
-        }
-        double cr[3];
-        cross3(rvi, rvj, cr);
-        double cn = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2] + 1e-15);
-        a += 0.5 * cn;
-        nrm[0] += cr[0] / cn;
-        nrm[1] += cr[1] / cn;
-        nrm[2] += cr[2] / cn;
-        rvi[0] = rvj[0];
-        rvi[1] = rvj[1];
-        rvi[2] = rvj[2];
-    }
-    double m = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
-    normal[0] = nrm[0] / m;
-    normal[1] = nrm[1] / m;
-    normal[2] = nrm[2] / m;
-    area = a;
-}
 
 // Adjoint of element_props: accumulate d(area)*areab + d(normal).normalb into
 // Xub of the face's vertices (atomically: vertices are shared between nodes).
@@ -150,45 +97,6 @@ __device__ void element_props_b(const double *Xu, const int *conn, int np, doubl
         atomicAdd(o + 1, rvb[k][1] + cb[1]);
         atomicAdd(o + 2, rvb[k][2] + cb[2]);
     }
-}
-
-__device__ __forceinline__ double mag_eps(const double *v) {
-    return sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2] + 1e-30);
-}
-
-constexpr double kRotTol = 1.4901161193847656e-08;
-
-// Rodrigues rotation taking direction v1 to direction v2 (row-major M).
-__device__ void rotation_matrix(const double *v1, const double *v2, double *M) {
-    double mag1 = mag_eps(v1), mag2 = mag_eps(v2);
-    double ax[3];
-    cross3(v1, v2, ax);
-    double axm = mag_eps(ax);
-    double s, omc;
-    if (axm < kRotTol) {
-        ax[0] = 1.0;
-        ax[1] = 0.0;
-        ax[2] = 0.0;
-        s = 0.0;
-        omc = 0.0;
-    } else {
-        ax[0] /= axm;
-        ax[1] /= axm;
-        ax[2] /= axm;
-        double d = (v1[0] / mag1) * (v2[0] / mag2) + (v1[1] / mag1) * (v2[1] / mag2) + (v1[2] / mag1) * (v2[2] / mag2);
-        double arg = (1.0 > d) ? d : 1.0;
-        double ang = acos(arg);
-        s = sin(ang);
-        omc = 1.0 - cos(ang);
-    }
-    double A[9] = {0.0, -ax[2], ax[1], ax[2], 0.0, -ax[0], -ax[1], ax[0], 0.0};
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            double C = A[3 * i] * A[j] + A[3 * i + 1] * A[3 + j] + A[3 * i + 2] * A[6 + j];
-            M[3 * i + j] = (i == j ? 1.0 : 0.0) + s * A[3 * i + j] + omc * C;
-        }
 }
 
 // Adjoint of rotation_matrix with respect to v2 (v1 = normals0 is fixed).
@@ -277,23 +185,6 @@ __device__ void node_normal_f(const SurfaceDev &s, int i, double &sumArea, doubl
         sumNormal[0] += dA * fp[1];
         sumNormal[1] += dA * fp[2];
         sumNormal[2] += dA * fp[3];
-    }
-}
-
-// Area-weighted node normal from the node's faces (kd_tree.F90:1603-1625).
-__device__ void node_normal(const SurfaceDev &s, const double *Xu, int i, double &sumArea, double *sumNormal) {
-    sumArea = 0.0;
-    sumNormal[0] = sumNormal[1] = sumNormal[2] = 0.0;
-    for (int e = s.n2ePtr[i]; e < s.n2ePtr[i + 1]; ++e) {
-        int f = s.n2e[e];
-        int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
-        double area, fn[3];
-        element_props(Xu, s.faceConn + f0, np, area, fn);
-        double dA = area / double(np);
-        sumArea += dA;
-        sumNormal[0] += dA * fn[0];
-        sumNormal[1] += dA * fn[1];
-        sumNormal[2] += dA * fn[2];
     }
 }
 

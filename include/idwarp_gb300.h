@@ -155,6 +155,20 @@ int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int whe
  * src/warp/warpMesh.F90:1-82) */
 int idw_warp_mesh(void *ctx);
 
+/* Complex step: the counterpart of the reference's complexified library
+ * (libidwarp_cs, loaded by idwarp/UnstructuredMesh_C.py; its
+ * setsurfacecoordinates / warpmesh / getvolumecoordinates take complex
+ * arrays).  coords holds 2*cdof doubles, the caller's (npts,3) complex
+ * coordinates with real and imaginary parts interleaved (numpy complex128
+ * layout); out receives 2*ndof doubles of the warped grid the same way.
+ * FP64 precision only (IDW_ERR_STATE otherwise).  The real part is the
+ * ordinary warp of the real coordinates; the imaginary part propagates the
+ * imaginary coordinates through the nodal properties in complex arithmetic
+ * and through the (linear) weighted sums of the same walk. */
+int idw_set_surface_coordinates_cs(void *ctx, const double *coords, int64_t cdof, int where);
+int idw_warp_mesh_cs(void *ctx);
+int idw_get_volume_coordinates_cs(void *ctx, double *out, int64_t ndof, int where);
+
 /* Warp nbatch surfaces (perturbations of the same surface definition) in one
  * call: coords holds nbatch stacked (npts,3) surfaces, out receives nbatch
  * stacked (nvol,3) grids.  In mixed precision up to four surfaces share one

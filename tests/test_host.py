@@ -141,10 +141,11 @@ def test_nonfinite_surface_coordinates_raise_error():
     assert m._surfVersion == 1
 
 
-def test_complex_step_classes_raise_a_clear_error():
-    # importable like the reference's, but the complex build is not on the GPU path
+def test_complex_step_classes_errors():
+    # USMesh_C runs the complex step in FP64 only; MultiUSMesh_C is not provided
     from idwarp_gb300 import Error, MultiUSMesh_C, USMesh_C
 
-    for cls in (USMesh_C, MultiUSMesh_C):
-        with pytest.raises(Error, match="warpDeriv"):
-            cls(options={})
+    with pytest.raises(Error, match="FP64"):
+        USMesh_C(options={"precision": "mixed"})
+    with pytest.raises(Error, match="USMesh_C"):
+        MultiUSMesh_C(options={})
