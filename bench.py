@@ -477,18 +477,29 @@ def run_suite():
     return 0
 
 
-def run_suite_d(steps=50):
+def run_suite_d(steps=50, sample=200000, directions=5):
     """Differentiation at scale: the two-body mesh (wing 577x261x53 + sphere
     158x79: 19.96M volume nodes, 302k surface points), 50 Adam steps on 48
     FFD coefficients minimising sum(1/max(V_cell, eps)) through the
-    differentiable warp (mixed precision), with the gradient checked against
-    central differences (h = 1e-6) on 5 random directions before the loop,
-    with the reference's rotation derivative and with rotations off."""
+    differentiable warp (mixed precision).  Gradient checks:
+      * central differences (h = 1e-6) on 5 random directions at the
+        undeformed surface, with the reference's rotation derivative (zero on
+        the degenerate rotation axes of an undeformed surface) and with
+        rotations off;
+      * the same at the deformed surface after the loop, where every wing
+        node's rotation axis is well defined;
+      * the GPU's reverse product against the oracle's (the reference's
+        warpDeriv restated, FP64) at the deformed surface: dXv = the
+        objective's gradient restricted to a seeded sample of volume nodes
+        (dXs is linear in dXv, so the sample's product is exact for that
+        dXv), compared over all surface points and along 5 random FFD
+        directions."""
     import torch
 
     from idwarp_gb300 import USMesh
     from idwarp_gb300 import synthetic as S
-    from idwarp_gb300.ffd import FFDBox, ffd_loop
+    from idwarp_gb300.autograd import warp
+    from idwarp_gb300.ffd import FFDBox, ffd_loop, inverse_volume_objective
 
     t0 = time.perf_counter()
     m = S.multibody()
@@ -506,13 +517,51 @@ def run_suite_d(steps=50):
     ffd = FFDBox(m["pts"], select=np.arange(m["nWingPts"]))
     xs0 = torch.tensor(m["pts"], device="cuda")
     cells = torch.tensor(m["cells"], device="cuda")
-    out = ffd_loop(g, xs0, cells, ffd, steps=steps, lr=1e-3, check_directions=5)
+    out = ffd_loop(g, xs0, cells, ffd, steps=steps, lr=1e-3, check_directions=directions)
     res.update({"objective_initial": out["initial"], "objective_final": out["objective"][-1],
                 "seconds": out["seconds"], "seconds_per_step": out["seconds_per_step"],
                 "gradient_check_rotations": out["gradient_check"]})
+    coef = torch.tensor(out["coef"], device="cuda")
+    res["coef_max_abs"] = float(coef.abs().max())
+    # FD at the deformed state (rotations on), starting the check there
+    chk = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions, coef0=coef)
+    res["gradient_check_rotations_deformed"] = chk["gradient_check"]
     g.setOption("useRotations", False)
-    out2 = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=5)
+    out2 = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions)
     res["gradient_check_no_rotations"] = out2["gradient_check"]
+    g.setOption("useRotations", True)
+    # the reverse product against the oracle on a volume sample, at the deformed state
+    B, sel = ffd.torch_operator(xs0.device)
+    xs = ffd.apply(xs0, coef, B, sel).detach()
+    xv = warp(xs, g).detach().requires_grad_(True)
+    f = inverse_volume_objective(xv, cells, 1e-12)
+    (gxv,) = torch.autograd.grad(f, xv)
+    rng = np.random.default_rng(301)
+    idx = np.sort(rng.choice(len(m["xv0"]), min(sample, len(m["xv0"])), replace=False))
+    gs = np.zeros(gxv.shape)
+    gs[idx] = gxv.cpu().numpy()[idx]
+    g.setSurfaceCoordinates(xs)
+    g.warpMesh()
+    g.warpDeriv(torch.tensor(gs.ravel(), device="cuda"), solverVec=False)
+    dxs_gpu = g.getdXs()
+    t0 = time.perf_counter()
+    smp = dict(m)
+    smp["xs"] = xs.cpu().numpy()
+    ors = OracleSample(smp, idx)
+    ors.step()
+    dxs_or = ors.om.warp_deriv(gs[idx])
+    res["oracle_seconds"] = time.perf_counter() - t0
+    scale = float(np.abs(dxs_or).max())
+    dirs = []
+    Bn = B.cpu().numpy()
+    for _ in range(directions):
+        d = rng.normal(size=ffd.nVars)
+        v = np.zeros(m["pts"].shape)
+        v[ffd.sel, 2] = Bn @ d
+        a, b = float(np.sum(dxs_gpu * v)), float(np.sum(dxs_or * v))
+        dirs.append({"gpu": a, "oracle": b, "rel": abs(a - b) / max(abs(b), 1e-300)})
+    res["adjoint_vs_oracle"] = {"sample_nodes": int(len(idx)), "max_rel_over_max_dXs":
+                                float(np.abs(dxs_gpu - dxs_or).max() / scale), "directions": dirs}
     res["peak_memory_GB"] = torch.cuda.max_memory_allocated() / 1e9
     print(json.dumps(res), flush=True)
     return 0

@@ -29,10 +29,14 @@ namespace {
 #define IDW_WALK_MIN_BLOCKS 8
 #endif
 
-template <int KIND>
+// STATS: count warp-level lane slots (diagnostics); EXACT: exact mode (every
+// leaf, no decisions).  Both are compile-time so that the product walk's loop
+// carries neither test.
+template <int KIND, int STATS, int EXACT>
 __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af,
                                                     VolumeDev v, WalkRecF rec, MixedParams mp, Law32<KIND> law,
-                                                    int exact, float4 *acc, unsigned long long *counters) {
+                                                    float4 *acc, unsigned long long *counters) {
+    constexpr int exact = EXACT;
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = gid < v.nVol;
     const int64_t g = valid ? gid : 0;
@@ -55,7 +59,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
         while (node < t.nNodes) {
             const int4 inf = ldgi4(&tf.nodes[node].info);
             const bool active = valid && node >= skip;
-            if (mp.slotStats && __any_sync(kFull, active) && counters && (threadIdx.x & 31) == 0)
+            if (STATS && __any_sync(kFull, active) && counters && (threadIdx.x & 31) == 0)
                 atomicAdd(counters + (inf.w ? 4 : 5), (unsigned long long)(inf.w ? 32 * (inf.y - inf.x + 1) : 32));
             if (inf.w) {
                 bool leafPrecise = false;
@@ -84,9 +88,14 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                     cnt.visited++;
                 }
                 if (__any_sync(kFull, leafPrecise)) {
-                    if (leafPrecise)
-                        precise_leaf<KIND>(tf, pf, node, inf.x, inf.y, rh, rl, law, Ls, LsLo, c1, mp.abH, mp.abL, sn,
-                                           cn, sd, cd);
+                    if (leafPrecise) {
+                        RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
+                        a = precise_leaf_ool<KIND>(a, tf, pf, node, inf.x, inf.y, rh[0], rh[1], rh[2], rl[0], rl[1],
+                                                   rl[2], law, Ls, LsLo, c1, mp.abH, mp.abL);
+                        sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
+                        cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
+                        sd = a.sd, cd = a.cd;
+                    }
                     warp_count(counters, 6, leafPrecise ? unsigned(inf.y - inf.x + 1) : 0u);
                 }
                 node = inf.z;
@@ -126,16 +135,14 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                 }
                 if (__any_sync(kFull, precise)) {
                     if (precise) {
-                        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
-                        dfl q[3];
-                        two_diff(rh[0], ch.x, q[0].h, q[0].l);
-                        two_diff(rh[1], ch.y, q[1].h, q[1].l);
-                        two_diff(rh[2], ch.z, q[2].h, q[2].l);
-                        q[0].l += rl[0] - cl.x;
-                        q[1].l += rl[1] - cl.y;
-                        q[2].l += rl[2] - cl.z;
-                        precise_term<KIND>(q, 0.f, cl.w, __ldg(&tf.nodes[node].aLo), af.dc + 12 * node,
-                                           af.dcl + 12 * node, law, Ls, LsLo, c1, mp.abH, mp.abL, sn, cn, sd, cd);
+                        RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
+                        a = precise_cluster<KIND>(a, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2],
+                                                  ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo),
+                                                  __ldg(&tf.nodes[node].aLo), af.dc + 12 * node, af.dcl + 12 * node,
+                                                  law, Ls, LsLo, c1, mp.abH, mp.abL);
+                        sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
+                        cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
+                        sd = a.sd, cd = a.cd;
                     }
                     warp_count(counters, 6, precise ? 1u : 0u);
                 }
@@ -212,6 +219,23 @@ __global__ void k_gate_den(int64_t nVol, const float4 *acc, float *gden) {
 
 inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
 
+template <int KIND>
+void launch_walk_kind(int g, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                      const VolumeDev &v, const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law,
+                      int exact, float4 *acc, unsigned long long *counters, cudaStream_t st) {
+    if (mp.slotStats) {
+        if (exact)
+            k_walk_mixed<KIND, 1, 1><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, acc, counters);
+        else
+            k_walk_mixed<KIND, 1, 0><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, acc, counters);
+    } else {
+        if (exact)
+            k_walk_mixed<KIND, 0, 1><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, acc, counters);
+        else
+            k_walk_mixed<KIND, 0, 0><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, acc, counters);
+    }
+}
+
 }  // namespace
 
 void launch_finalize_mixed(const VolumeDev &v, const WalkRecF &rec, const float4 *acc, double bExp, double *xv,
@@ -265,14 +289,13 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
         // every pair: the tiled kernel, with the walk's arithmetic
         launch_exact_mixed(tf, pf, af, v, rec, mp, k.law, acc, o.counters, st);
     } else if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
-        Law32<0> law{3, 5, 3.f, 5.f};
-        k_walk_mixed<0><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
+        launch_walk_kind(g, t, tf, pf, af, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, acc, o.counters, st);
     } else if (k.law.isInt) {
-        Law32<1> law{k.law.ia, k.law.ib, float(k.law.aExp), float(k.law.bExp)};
-        k_walk_mixed<1><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
+        launch_walk_kind(g, t, tf, pf, af, v, rec, mp, Law32<1>{k.law.ia, k.law.ib, float(k.law.aExp), float(k.law.bExp)},
+                         exact, acc, o.counters, st);
     } else {
-        Law32<2> law{0, 0, float(k.law.aExp), float(k.law.bExp)};
-        k_walk_mixed<2><<<g, 128, 0, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, o.counters);
+        launch_walk_kind(g, t, tf, pf, af, v, rec, mp, Law32<2>{0, 0, float(k.law.aExp), float(k.law.bExp)}, exact,
+                         acc, o.counters, st);
     }
     k_finalize_mixed<<<blocks(v.nVol, 256), 256, 0, st>>>(v, rec, acc, k.law.bExp, o.tangent, o.xv,
                                                           o.tangent ? nullptr : o.den);

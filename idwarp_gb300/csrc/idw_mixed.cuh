@@ -308,6 +308,18 @@ __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const floa
     return (err + bnd < tauf) ? 1 : ((err - bnd > tauf) ? 0 : 2);
 }
 
+// The FP64 decision of one lane, out of line: it is rare (about one visit in
+// 1e5), and keeping its FP64 code out of the walks' loops keeps their
+// register allocation to the FP32 path.
+static __device__ __noinline__ int decide64_lane(const dbl4 *geom, const double *err, const int *perm, const double *den0,
+                                          int64_t g, int node, float rh0, float rh1, float rh2, float rl0,
+                                          float rl1, float rl2, double errTol) {
+    const int vi = perm[g];
+    const double r[3] = {double(rh0) + double(rl0), double(rh1) + double(rl1), double(rh2) + double(rl2)};
+    double dist64;
+    return decide64(geom[node], err + kNerr * node, r, errTol * den0[vi], dist64);
+}
+
 // Re-take undecided decisions with the FP64 rule (all lanes of the warp call
 // this; the FP64 work runs only when some lane needs it).
 __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const VolumeDev &v, int64_t g, int node,
@@ -315,12 +327,8 @@ __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const Volume
                                          unsigned long long *counters) {
     if (__any_sync(kFull, dec == 2)) {
         const bool redo = dec == 2;
-        if (redo) {
-            const int vi = v.perm[g];
-            double r[3] = {double(rh[0]) + double(rl[0]), double(rh[1]) + double(rl[1]), double(rh[2]) + double(rl[2])};
-            double dist64;
-            dec = decide64(t.geom[node], t.err + kNerr * node, r, errTol * v.den0[vi], dist64);
-        }
+        if (redo) dec = decide64_lane(t.geom, t.err, v.perm, v.den0, g, node, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2],
+                                      errTol);
         warp_count(counters, 3, redo ? 1u : 0u);
     }
     return dec;
@@ -472,6 +480,44 @@ __device__ __forceinline__ void precise_leaf(const TreeDevF &tf, const PointsDev
         precise_term<KIND>(x, 1e-15f, da.w, dl.w, pf.dm + 12 * i, pf.dml + 12 * i, law, Ls, LsLo, c1, abH, abL, sn,
                            cn, sd, cd);
     }
+}
+
+// Running sums of one mirror pass (num 3 + den, each a compensated pair),
+// passed by value to the out-of-line double-float paths below so that the
+// walks keep them in registers.
+struct RunSums {
+    float sn[3], cn[3], sd, cd;
+};
+
+// A cluster term in double-float (the walk's precision gate sent it here):
+// h + l is the split volume point, ch/cl the split centroid (cl.w = area hi),
+// aLo the area's low part, dc/dcl the cluster's D', c' hi/lo.  Out of line,
+// like precise_leaf: rare, and register-heavy.
+template <int KIND>
+__device__ __noinline__ RunSums precise_cluster(RunSums a, float rh0, float rh1, float rh2, float rl0, float rl1,
+                                                float rl2, float4 ch, float4 cl, float aLo, const float *dc,
+                                                const float *dcl, Law32<KIND> law, float Ls, float LsLo, float c1,
+                                                float abH, float abL) {
+    dfl q[3];
+    two_diff(rh0, ch.x, q[0].h, q[0].l);
+    two_diff(rh1, ch.y, q[1].h, q[1].l);
+    two_diff(rh2, ch.z, q[2].h, q[2].l);
+    q[0].l += rl0 - cl.x;
+    q[1].l += rl1 - cl.y;
+    q[2].l += rl2 - cl.z;
+    precise_term<KIND>(q, 0.f, cl.w, aLo, dc, dcl, law, Ls, LsLo, c1, abH, abL, a.sn, a.cn, a.sd, a.cd);
+    return a;
+}
+
+// precise_leaf out of line, on the running sums by value.
+template <int KIND>
+__device__ __noinline__ RunSums precise_leaf_ool(RunSums a, const TreeDevF tf, const PointsDevF pf, int node, int lo,
+                                                 int hi, float rh0, float rh1, float rh2, float rl0, float rl1,
+                                                 float rl2, Law32<KIND> law, float Ls, float LsLo, float c1, float abH,
+                                                 float abL) {
+    const float rh[3] = {rh0, rh1, rh2}, rl[3] = {rl0, rl1, rl2};
+    precise_leaf<KIND>(tf, pf, node, lo, hi, rh, rl, law, Ls, LsLo, c1, abH, abL, a.sn, a.cn, a.sd, a.cd);
+    return a;
 }
 
 // End of one mirror pass: add the reference motion back, num += den (Dref r +

@@ -71,15 +71,20 @@ def inverse_volume_objective(xv, cells, eps):
     return torch.sum(1.0 / torch.clamp(hex_volumes(xv, cells), min=eps))
 
 
-def ffd_loop(mesh, xs0, cells, ffd, steps=50, lr=1e-3, eps=1e-12, check_directions=5, fd_step=1e-6, seed=300):
+def ffd_loop(mesh, xs0, cells, ffd, steps=50, lr=1e-3, eps=1e-12, check_directions=5, fd_step=1e-6, seed=300,
+             coef0=None):
     """Gradient steps (Adam) on the FFD coefficients minimising
-    sum(1 / max(V_cell, eps)) of the warped grid.  Before the loop the
-    gradient is checked against central differences on ``check_directions``
-    random directions.  Returns a dict with the objective history, the
-    gradient check and timings."""
+    sum(1 / max(V_cell, eps)) of the warped grid, from ``coef0`` (zero by
+    default: the undeformed surface).  Before the loop the gradient is
+    checked against central differences on ``check_directions`` random
+    directions.  Returns a dict with the objective history, the gradient
+    check and timings."""
     dev = xs0.device
     B, sel = ffd.torch_operator(dev)
-    coef = torch.zeros(ffd.nVars, dtype=torch.float64, device=dev, requires_grad=True)
+    if coef0 is None:
+        coef = torch.zeros(ffd.nVars, dtype=torch.float64, device=dev, requires_grad=True)
+    else:
+        coef = torch.as_tensor(coef0, dtype=torch.float64, device=dev).clone().requires_grad_(True)
 
     def objective(c):
         return inverse_volume_objective(warp(ffd.apply(xs0, c, B, sel), mesh), cells, eps)
@@ -92,8 +97,8 @@ def ffd_loop(mesh, xs0, cells, ffd, steps=50, lr=1e-3, eps=1e-12, check_directio
     with torch.no_grad():
         for _ in range(check_directions):
             d = torch.tensor(rng.normal(size=ffd.nVars), device=dev)
-            fp = objective(fd_step * d).item()
-            fm = objective(-fd_step * d).item()
+            fp = objective(coef + fd_step * d).item()
+            fm = objective(coef - fd_step * d).item()
             fd = (fp - fm) / (2 * fd_step)
             ad = float(torch.dot(g0, d))
             check.append({"ad": ad, "fd": fd, "rel": abs(ad - fd) / max(abs(fd), 1e-300)})

@@ -75,7 +75,7 @@ def lib(path=None):
     p = os.path.abspath(path or build_oracle())
     if p not in _libs:
         _libs[p] = _bind(C.CDLL(p))
-    if path is None or _lib is None:
+    if path is None:
         _lib = _libs[p]
     return _libs[p]
 
