@@ -793,14 +793,7 @@ def main():
             if rc != 0:
                 _lib.check(L, msh.ctx, rc, "warpDerivBatch")
 
-        deriv(mesh, dxs)  # warm-up
-        barrier()
-        e0.record(stream)
-        for _ in range(3):
-            deriv(mesh, dxs)
-        e1.record(stream)
-        barrier()
-        msd = e0.elapsed_time(e1) / 3
+        # FP64 plain form (one launch of 16 seeds)
         barrier()
         e0.record(stream)
         deriv(m64, dxs64)
@@ -808,11 +801,7 @@ def main():
         barrier()
         msd64 = e0.elapsed_time(e1)
         dref = dxs64.abs().max().item()
-        out["warpDeriv"] = {"seeds": 16, "value": 16 * nvol / (msd * 1e-3), "unit": "seeds*nodes/s",
-                            "ms": msd, "precision": "mixed",
-                            "fp64_value": 16 * nvol / (msd64 * 1e-3), "fp64_ms": msd64,
-                            "speedup_mixed_over_fp64": msd64 / msd,
-                            "max_rel_diff_vs_fp64": float((dxs - dxs64).abs().max().item() / dref)}
+        d1ref = dxs64[0].abs().max().item()
 
         # one seed (the solver-adjoint call pattern): idw_warp_deriv on the device
         def deriv1():
@@ -820,18 +809,39 @@ def main():
             if rc != 0:
                 _lib.check(L, mesh.ctx, rc, "warpDeriv")
 
-        deriv1()
-        barrier()
-        e0.record(stream)
-        for _ in range(5):
+        # the mixed adjoint in both forms: double-float (default) and FP32
+        res16, res1 = {}, {}
+        for adj in ("precise", "fast"):
+            mesh.setOption("adjointPrecision", adj)
+            mesh._setMeshOptions()
+            deriv(mesh, dxs)  # warm-up (the precise form's denominator walk runs once here)
+            barrier()
+            e0.record(stream)
+            for _ in range(3):
+                deriv(mesh, dxs)
+            e1.record(stream)
+            barrier()
+            msd = e0.elapsed_time(e1) / 3
+            res16[adj] = {"seeds": 16, "value": 16 * nvol / (msd * 1e-3), "unit": "seeds*nodes/s", "ms": msd,
+                          "adjointPrecision": adj, "speedup_mixed_over_fp64": msd64 / msd,
+                          "max_rel_diff_vs_fp64": float((dxs - dxs64).abs().max().item() / dref)}
             deriv1()
-        e1.record(stream)
-        barrier()
-        ms1 = e0.elapsed_time(e1) / 5
-        d1 = torch.tensor(mesh.getdXs(), device="cuda")
-        out["warpDeriv1"] = {"seeds": 1, "value": nvol / (ms1 * 1e-3), "unit": "seeds*nodes/s", "ms": ms1,
-                             "max_rel_diff_vs_fp64": float((d1 - dxs64[0]).abs().max().item()
-                                                           / dxs64[0].abs().max().item())}
+            barrier()
+            e0.record(stream)
+            for _ in range(5):
+                deriv1()
+            e1.record(stream)
+            barrier()
+            ms1 = e0.elapsed_time(e1) / 5
+            d1 = torch.tensor(mesh.getdXs(), device="cuda")
+            res1[adj] = {"seeds": 1, "value": nvol / (ms1 * 1e-3), "unit": "seeds*nodes/s", "ms": ms1,
+                         "adjointPrecision": adj,
+                         "max_rel_diff_vs_fp64": float((d1 - dxs64[0]).abs().max().item() / d1ref)}
+        mesh.setOption("adjointPrecision", "precise")
+        mesh._setMeshOptions()
+        out["warpDeriv"] = dict(res16["precise"], fp64_value=16 * nvol / (msd64 * 1e-3), fp64_ms=msd64,
+                                fast=res16["fast"])
+        out["warpDeriv1"] = dict(res1["precise"], fast=res1["fast"])
         del sd, dxs, dxs64, d1
         # 8 independent surface perturbations (seeds 200-207) through the batched
         # walk (four surfaces share one tree walk) against one warpMesh each

@@ -3,13 +3,23 @@
 Drop-in for ``idwarp.MultiUSMesh`` (idwarp/MultiUnstructuredMesh.py:47-892)
 without the CGNS layer.  The reference reads one combined CGNS file, groups
 its domains by name (one IDWarp instance per group) and leaves the groups
-without options as a fixed background.  Here the combined grid is given as an
-ordered list of ``(name, volNodes, nBlocks)`` groups: ``volNodes`` (N, 3) are
-the group's nodes in combined order and ``nBlocks`` the number of CGNS-like
-blocks it spans, so that surface elements are routed by block ID exactly as
-the reference does (:462-597).  Each warped group is a
+without options as a fixed background.  Here the combined grid is either
+
+* a multi-block PLOT3D file (the reference's constructor shape,
+  ``MultiUSMesh(gridFile, optionsDict, comm)``) whose blocks carry names in
+  the cgns_utils combine convention ``<zone>.<index>`` (``blockNames``, or one
+  name per line in ``<gridFile>.names``); consecutive blocks of one zone form
+  a group, as the reference's explodeByZoneName does; or
+* an ordered list of ``(name, volNodes, nBlocks)`` groups: ``volNodes``
+  (N, 3) are the group's nodes in combined order and ``nBlocks`` the number
+  of blocks it spans.
+
+Surface elements are routed to the groups by block ID exactly as the
+reference does (:462-597).  Each warped group is a
 :class:`~idwarp_gb300.USMesh` on the GPU.
 """
+import os
+
 import numpy as np
 
 from .options import Error
@@ -19,9 +29,11 @@ from .UnstructuredMesh import USMesh
 class MultiUSMesh:
     """Several IDWarp instances behind one solver-facing interface."""
 
-    def __init__(self, grids, optionsDict, comm=None, dtype="d", debug=False):
+    def __init__(self, grids, optionsDict, comm=None, dtype="d", debug=False, blockNames=None):
         if optionsDict is None:
             raise Error("optionsDict is not optional: one options dictionary per warped group.")
+        if isinstance(grids, (str, os.PathLike)):
+            grids = zone_groups_from_plot3d(grids, blockNames)
         self.comm = comm
         self.dtype = dtype
         self.meshes = []
@@ -175,3 +187,36 @@ class MultiUSMesh:
                 except Exception:
                     pass
         self.meshes = []
+
+
+def zone_groups_from_plot3d(gridFile, blockNames=None):
+    """(name, volNodes, nBlocks) groups of a multi-block PLOT3D grid: blocks
+    named ``<zone>.<index>`` (cgns_utils combine), or plain zone names,
+    grouped by zone in file order; ``blockNames`` defaults to the lines of
+    ``<gridFile>.names``."""
+    from .plot3d import readPlot3D
+
+    nodes, sizes = readPlot3D(os.fspath(gridFile), return_blocks=True)
+    if blockNames is None:
+        sidecar = os.fspath(gridFile) + ".names"
+        if not os.path.exists(sidecar):
+            raise Error("MultiUSMesh needs the block names of %s: pass blockNames or write one name per block in %s"
+                        % (gridFile, sidecar))
+        with open(sidecar) as f:
+            blockNames = [ln.strip() for ln in f if ln.strip()]
+    if len(blockNames) != len(sizes):
+        raise Error("%d block names for %d blocks in %s" % (len(blockNames), len(sizes), gridFile))
+    counts = [int(a) * int(b) * int(c) for a, b, c in sizes]
+    groups = []
+    off = 0
+    for name, n in zip(blockNames, counts):
+        zone = name.rsplit(".", 1)[0] if "." in name else name
+        if groups and groups[-1][0] == zone:
+            groups[-1][1].append(nodes[off:off + n])
+            groups[-1][2] += 1
+        else:
+            if any(g[0] == zone for g in groups):
+                raise Error("the blocks of zone %r are not consecutive in %s" % (zone, gridFile))
+            groups.append([zone, [nodes[off:off + n]], 1])
+        off += n
+    return [(zone, np.concatenate(parts), nb) for zone, parts, nb in groups]

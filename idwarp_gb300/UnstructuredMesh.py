@@ -102,6 +102,7 @@ class USMesh(BaseSolver):
             "mixedGate": [float, 2e-3],
             "diagnostics": [int, 0],
             "exactSchedule": [str, ["auto", "tiled", "walk"]],
+            "adjointPrecision": [str, ["precise", "fast"]],
         }
 
     # ------------------------------------------------------------------
@@ -547,6 +548,7 @@ class USMesh(BaseSolver):
         o.mixedGate = self.getOption("mixedGate")
         o.diagnostics = self.getOption("diagnostics")
         o.exactSchedule = {"auto": 0, "tiled": 1, "walk": 2}[self.getOption("exactSchedule")]
+        o.adjointPrecision = {"precise": _lib.IDW_ADJ_PRECISE, "fast": _lib.IDW_ADJ_FAST}[self.getOption("adjointPrecision")]
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

@@ -16,6 +16,8 @@ IDW_EVAL_EXACT = 0
 IDW_EVAL_FAST = 1
 IDW_PREC_FP64 = 0
 IDW_PREC_MIXED = 1
+IDW_ADJ_PRECISE = 0
+IDW_ADJ_FAST = 1
 IDW_OK = 0
 IDW_ERR_ARG = -1
 IDW_ERR_STATE = -2
@@ -37,7 +39,8 @@ class idw_options(C.Structure):
         ("errTol", C.c_double), ("symmTol", C.c_double), ("cornerAngle", C.c_double),
         ("evalMode", C.c_int32), ("useRotations", C.c_int32), ("zeroCornerRotations", C.c_int32),
         ("bucketSize", C.c_int32), ("precision", C.c_int32), ("diagnostics", C.c_int32),
-        ("mixedGate", C.c_double), ("exactSchedule", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("mixedGate", C.c_double), ("exactSchedule", C.c_int32), ("adjointPrecision", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

@@ -378,6 +378,14 @@ void launch_adj_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, 
 
 }  // namespace
 
+void launch_adjoint_combine(const TreeDev &t, const dbl4 *ptXA, int nPts, int nSeeds, const double *ptAcc,
+                            const double *nodeAcc, double *ptAdj, cudaStream_t st) {
+    const int64_t total = int64_t(nPts) * nSeeds;
+    if (total <= 0) return;
+    k_adjoint_combine<<<int((total + 127) / 128), 128, 0, st>>>(t, ptXA, nPts, nSeeds, ptAcc, 12 * int64_t(nPts),
+                                                                nodeAcc, 12 * int64_t(t.nNodes), ptAdj);
+}
+
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,

@@ -93,6 +93,11 @@ struct Ctx {
     bool gdenValid = false;
     double gdenLdefFact = 0.0, gdenAlpha = 0.0;
     int gdenMode = -1;
+    // the precise adjoint's denominator (double-float weights), per law and mode
+    DevBuf<double> denP;
+    bool denPValid = false;
+    double denPLdefFact = 0.0, denPAlpha = 0.0;
+    int denPMode = -1;
     DevBuf<float> ptDM, ptDMl, nodeDC, nodeDCl, nodeDn, refDB;
     // adjoint
     DevBuf<double> ptAdj, nodeAdj, xub, dxs;
@@ -245,6 +250,8 @@ int validate_options(Ctx *c, const idw_options *o) {
     if (!(o->mixedGate >= 0.0)) return fail(c, IDW_ERR_ARG, "mixedGate must be >= 0");
     if (o->exactSchedule < IDW_EXACT_AUTO || o->exactSchedule > IDW_EXACT_WALK)
         return fail(c, IDW_ERR_ARG, "exactSchedule must be IDW_EXACT_AUTO, IDW_EXACT_TILED or IDW_EXACT_WALK");
+    if (o->adjointPrecision != IDW_ADJ_PRECISE && o->adjointPrecision != IDW_ADJ_FAST)
+        return fail(c, IDW_ERR_ARG, "adjointPrecision must be IDW_ADJ_PRECISE or IDW_ADJ_FAST");
     return IDW_OK;
 }
 
@@ -271,6 +278,7 @@ int finish_den0(Ctx *c) {
     int e = check_launch(c, "walk records");
     if (e) return e;
     c->gdenValid = false;
+    c->denPValid = false;
     c->den0Valid = true;
     return IDW_OK;
 }
@@ -312,6 +320,7 @@ void idw_default_options(idw_options *o) {
     o->precision = IDW_PREC_MIXED;
     o->diagnostics = 0;
     o->mixedGate = 2e-3;
+    o->adjointPrecision = IDW_ADJ_PRECISE;
 }
 
 int idw_create(const idw_options *opts, void **ctx_out) {
@@ -659,6 +668,7 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->acc.alloc(2 * size_t(c->nVol)));
     CKA(c->gden.alloc(size_t(c->nVol)));
     c->gdenValid = false;
+    c->denPValid = false;
     c->den0Valid = false;
     CK(cudaStreamSynchronize(st));
     c->haveTree = true;
@@ -1227,8 +1237,29 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
-        launch_adjoint_mixed(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride, c->den.p,
-                             ptAdj.p, nodeAdj.p, ptRel.p, c->ptXA.p, n, c->counters.p, c->stream, c->adjMaxGroup);
+        if (c->opt.adjointPrecision == IDW_ADJ_PRECISE && precise_adjoint_supported(k.law)) {
+            // the denominator to double-float accuracy: once per weight law and mode
+            if (!(c->denPValid && c->denPLdefFact == c->opt.LdefFact && c->denPAlpha == c->opt.alpha &&
+                  c->denPMode == c->opt.evalMode)) {
+                CKA(c->denP.alloc(size_t(c->nVol)));
+                launch_precise_denominator(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, c->denP.p, c->stream);
+                rc = check_launch(c, "precise denominator");
+                if (rc) return rc;
+                c->denPValid = true;
+                c->denPLdefFact = c->opt.LdefFact;
+                c->denPAlpha = c->opt.alpha;
+                c->denPMode = c->opt.evalMode;
+                CK(cudaEventRecord(c->ev0, c->stream));
+            }
+            launch_adjoint_precise(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride,
+                                   c->denP.p, ptAdj.p, nodeAdj.p, n, c->counters.p, c->stream);
+            // the relative moments and the cluster shares, as the FP32 walk's
+            launch_adjoint_combine(tree_dev(c), c->ptXA.p, n, nSeeds, ptAdj.p, nodeAdj.p, ptRel.p, c->stream);
+        } else {
+            launch_adjoint_mixed(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride, c->den.p,
+                                 ptAdj.p, nodeAdj.p, ptRel.p, c->ptXA.p, n, c->counters.p, c->stream,
+                                 c->adjMaxGroup);
+        }
     } else {
         launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride,
                                  ptAdj.p, nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
@@ -1755,6 +1786,10 @@ int idw_autotune(void *ctx, int32_t nsurfaces, int32_t nseeds, idw_tuning *out) 
         const int groups[3] = {16, 8, 4};
         float best = 0.f;
         const int keep = c->adjMaxGroup;
+        // the seed groups are those of the FP32 form of the adjoint (the
+        // double-float form has its own fixed groups of 16, 4 and 1)
+        const int keepPrec = c->opt.adjointPrecision;
+        c->opt.adjointPrecision = IDW_ADJ_FAST;
         for (int q = 0; q < 3; ++q) {
             c->adjMaxGroup = groups[q];
             float ms = 0.f;
@@ -1768,6 +1803,7 @@ int idw_autotune(void *ctx, int32_t nsurfaces, int32_t nseeds, idw_tuning *out) 
             }
         }
         c->adjMaxGroup = rc ? keep : out->adjMaxGroup;
+        c->opt.adjointPrecision = keepPrec;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

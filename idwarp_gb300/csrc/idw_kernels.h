@@ -216,6 +216,20 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
                          const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st,
                          int maxGroup = 16);
+// Point and cluster moments of a mixed reverse walk -> the relative point
+// adjoints of the reverse nodal properties (setData_b folded in).
+void launch_adjoint_combine(const TreeDev &t, const dbl4 *ptXA, int nPts, int nSeeds, const double *ptAcc,
+                            const double *nodeAcc, double *ptAdj, cudaStream_t st);
+// Precise (double-float) mixed reverse walk and its denominator walk
+// (idw_adjoint_precise.cu); integer exponents only.
+bool precise_adjoint_supported(const WeightLaw &wl);
+void launch_precise_denominator(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
+                                const WalkRecF &rec, const EvalConsts &k, int exact, double *denOut,
+                                cudaStream_t st);
+int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
+                           const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
+                           int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, int nPts,
+                           unsigned long long *counters, cudaStream_t st);
 int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
                 cudaStream_t st);
 

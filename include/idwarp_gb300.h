@@ -53,6 +53,9 @@ extern "C" {
 #define IDW_EXACT_TILED 1 /* shared-memory tiles of surface points, several volume nodes per thread */
 #define IDW_EXACT_WALK 2  /* the tree walk with every node opened */
 
+#define IDW_ADJ_PRECISE 0 /* mixed warpDeriv in double-float (FP32 pairs): terms, products and lane sums */
+#define IDW_ADJ_FAST 1    /* mixed warpDeriv with FP32 weights, products and lane sums */
+
 /* Mesh options: the gridinput module variables (src/modules/gridInput.f90:9-18,
  * libidwarp.pyf:148-162) plus kd_tree.bucket_size (libidwarp.pyf:204-206) and
  * the GB300 precision switch.  Semantics follow doc/options.yaml. */
@@ -78,7 +81,10 @@ typedef struct idw_options {
     int32_t exactSchedule; /* mixed exact mode: IDW_EXACT_AUTO (default: tiled
                             * kernel when the mesh fills the GPU, else the walk),
                             * IDW_EXACT_TILED or IDW_EXACT_WALK; same sums either way */
-    int32_t reserved[3];
+    int32_t adjointPrecision; /* mixed warpDeriv: IDW_ADJ_PRECISE (default) or
+                               * IDW_ADJ_FAST (FP32 terms, a few 1e-7 relative per
+                               * term; real-valued exponents always use FP32) */
+    int32_t reserved[2];
 } idw_options;
 
 /* Work counters of the last warp / warpDeriv call. */
@@ -218,7 +224,9 @@ int idw_warp_deriv_fwd(void *ctx, const double *dxs, int64_t cdof, double *dxv, 
  * counterpart (the reference takes one direction per call). */
 int idw_warp_deriv_fwd_batch(void *ctx, const double *dxs, int32_t ndir, double *dxv, int where);
 
-/* idw_warp_deriv for one seed without allocating device memory in the call,
+/* idw_warp_deriv for one seed without allocating device memory in the call
+ * (in mixed precision its FP32 form, IDW_ADJ_FAST: the double-float form's
+ * denominator array would need an allocation),
  * for callers that cannot allocate while they run (memory reserved up front,
  * allocation-free solver loops).  No reference counterpart.  dxv (nvol,3)
  * and dxs (npts,3, receives the result) are device pointers; the work is
@@ -285,7 +293,7 @@ int idw_get_nodal_properties(void *ctx, double *mi, double *bi);
 /* Launch shapes chosen by idw_autotune, and the candidates' times. */
 typedef struct idw_tuning {
     int32_t batchGroup;  /* surfaces per batched walk (1..4) */
-    int32_t adjMaxGroup; /* largest seed group per adjoint walk (16, 8 or 4) */
+    int32_t adjMaxGroup; /* largest seed group per walk of the FP32 adjoint (16, 8 or 4) */
     double batchMs[4];   /* nsurfaces warps with 1..4 surfaces per walk */
     double adjMs[3];     /* nseeds reverse products with groups of 16, 8, 4 */
     int32_t reserved[4];

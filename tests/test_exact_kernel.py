@@ -111,14 +111,15 @@ def _deriv(m, opts, precision, dxv):
 
 @pytest.mark.parametrize("which,planes", [("wing", 0), ("sphere", 3)])
 def test_tiled_exact_adjoint(which, planes, built_lib):
-    # the reverse product in exact mode: tiled (per-warp moment reduction)
-    # against the walk and against the FP64 form; sums in another order, so
-    # within the mixed form's tolerance rather than bitwise
+    # the reverse product in exact mode (the FP32 form, whose one-seed calls
+    # the tiled kernel serves): tiled (per-warp moment reduction) against the
+    # walk and against the FP64 form; sums in another order, so within the
+    # FP32 form's tolerance rather than bitwise
     m = _mesh(which, planes)
     dxv = np.random.default_rng(71).normal(size=3 * len(m["xv0"]))
     ref = _deriv(m, {}, "fp64", dxv)
-    tiled = _deriv(m, {"exactSchedule": "tiled"}, "mixed", dxv)
-    walk = _deriv(m, {"exactSchedule": "walk"}, "mixed", dxv)
+    tiled = _deriv(m, {"exactSchedule": "tiled", "adjointPrecision": "fast"}, "mixed", dxv)
+    walk = _deriv(m, {"exactSchedule": "walk", "adjointPrecision": "fast"}, "mixed", dxv)
     scale = np.abs(ref).max()
     assert np.abs(tiled - walk).max() <= 1e-6 * scale
     assert np.abs(tiled - ref).max() <= 1e-6 * scale
@@ -127,8 +128,8 @@ def test_tiled_exact_adjoint(which, planes, built_lib):
 def test_tiled_exact_adjoint_several_seeds(built_lib):
     m = wing_small()
     dxv = np.random.default_rng(72).normal(size=(3, len(m["xv0"]), 3))
-    tiled = _deriv(m, {"exactSchedule": "tiled"}, "mixed", dxv)
-    walk = _deriv(m, {"exactSchedule": "walk"}, "mixed", dxv)
+    tiled = _deriv(m, {"exactSchedule": "tiled", "adjointPrecision": "fast"}, "mixed", dxv)
+    walk = _deriv(m, {"exactSchedule": "walk", "adjointPrecision": "fast"}, "mixed", dxv)
     assert tiled.shape == walk.shape
     assert np.abs(tiled - walk).max() <= 1e-6 * np.abs(walk).max()
 

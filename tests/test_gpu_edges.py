@@ -115,9 +115,10 @@ def test_mixed_derivatives_extreme_cases(opts, planes, built_lib):
         g.warpMesh()
         g.warpDeriv(dxv, solverVec=False)
         out[precision] = (g.getdXs(), g.warpDerivFwd(dxs, solverVec=False))
-    for k in range(2):
+    # reverse product: the double-float adjoint; tangent: the FP32 walk
+    for k, tol in ((0, 1e-9), (1, 1e-6)):
         ref = out["fp64"][k]
-        assert np.abs(out["mixed"][k] - ref).max() <= 1e-6 * np.abs(ref).max(), k
+        assert np.abs(out["mixed"][k] - ref).max() <= tol * np.abs(ref).max(), k
 
 
 def test_nonfinite_volume_grid_raises(sphere, built_lib):

@@ -193,6 +193,9 @@ def test_errors_are_raised(sphere, built_lib):
 
 
 TOL_MIXED = 1e-8  # max |mixed - FP64| / Ldef (precision error on the same tree and decisions)
+# warpDeriv, max |mixed - FP64| / max |dXs|: the double-float adjoint (the
+# default) and the FP32 one (adjointPrecision "fast")
+TOL_DERIV = {"precise": 1e-9, "fast": 1e-6}
 
 
 @pytest.mark.parametrize("mode", ["fast", "exact"])
@@ -240,10 +243,13 @@ def test_mixed_general_exponents(sphere, built_lib, oracle_lib):
             assert err < tol, (a, b, err)
 
 
-def test_mixed_denominator_feeds_deriv(wing, built_lib, oracle_lib):
-    # warpDeriv after a mixed warpMesh uses the mixed run's (unscaled) denominator
+@pytest.mark.parametrize("adj", ["precise", "fast"])
+def test_mixed_deriv_matches_oracle(adj, wing, built_lib, oracle_lib):
+    # the mixed warpDeriv against the oracle: the fast form divides by the
+    # mixed warp's denominator (FP32 weights, ~1e-7 relative per node), the
+    # precise form by its own double-float denominator
     om = build_oracle(wing)
-    g = build_gpu(wing, precision="mixed")
+    g = build_gpu(wing, {"adjointPrecision": adj}, precision="mixed")
     om.set_surface_coordinates(wing["xs"])
     g.setSurfaceCoordinates(wing["xs"])
     om.warp()
@@ -252,16 +258,16 @@ def test_mixed_denominator_feeds_deriv(wing, built_lib, oracle_lib):
     dxv = rng.normal(size=wing["xv0"].shape)
     do = om.warp_deriv(dxv)
     g.warpDeriv(dxv.ravel(), solverVec=False)
-    # the mixed denominator carries FP32 rounding (~1e-7 relative per node)
-    assert np.abs(g.getdXs() - do).max() <= 1e-6 * np.abs(do).max()
+    err = np.abs(g.getdXs() - do).max() / np.abs(do).max()
+    assert err <= TOL_DERIV[adj], err
 
 
-def test_mixed_deriv_every_seed_group(wing, built_lib):
-    # 29 seeds = groups of 16, 8, 4 and 1: every form of the mixed adjoint's
-    # warp reduction (blocked, lane groups, per-task lanes, shuffles) against
-    # the FP64 adjoint
+@pytest.mark.parametrize("adj", ["precise", "fast"])
+def test_mixed_deriv_every_seed_group(adj, wing, built_lib):
+    # 29 seeds = groups of 16, 8, 4 and 1 (fast) or 16, 4, 4, 4, 1 (precise):
+    # every form of the mixed adjoint's warp reduction against the FP64 adjoint
     g64 = build_gpu(wing, precision="fp64")
-    g32 = build_gpu(wing, precision="mixed")
+    g32 = build_gpu(wing, {"adjointPrecision": adj}, precision="mixed")
     seeds = np.random.default_rng(19).normal(size=(29,) + wing["xv0"].shape)
     out = []
     for g in (g64, g32):
@@ -270,14 +276,15 @@ def test_mixed_deriv_every_seed_group(wing, built_lib):
         out.append(g.warpDerivBatch(seeds))
     for lo, hi in ((0, 16), (16, 24), (24, 28), (28, 29)):
         ref = out[0][lo:hi]
-        assert np.abs(out[1][lo:hi] - ref).max() <= 1e-6 * np.abs(ref).max(), (lo, hi)
+        assert np.abs(out[1][lo:hi] - ref).max() <= TOL_DERIV[adj] * np.abs(ref).max(), (lo, hi)
 
 
+@pytest.mark.parametrize("adj", ["precise", "fast"])
 @pytest.mark.parametrize("mode", ["fast", "exact"])
-def test_mixed_deriv_batch_matches_fp64(mode, wing, built_lib):
+def test_mixed_deriv_batch_matches_fp64(mode, adj, wing, built_lib):
     # the mixed adjoint (S seeds sharing one walk) against the FP64 adjoint
     g64 = build_gpu(wing, {"evalMode": mode}, precision="fp64")
-    g32 = build_gpu(wing, {"evalMode": mode}, precision="mixed")
+    g32 = build_gpu(wing, {"evalMode": mode, "adjointPrecision": adj}, precision="mixed")
     rng = np.random.default_rng(9)
     seeds = rng.normal(size=(6,) + wing["xv0"].shape)
     out = []
@@ -286,7 +293,7 @@ def test_mixed_deriv_batch_matches_fp64(mode, wing, built_lib):
         g.warpMesh()
         out.append(g.warpDerivBatch(seeds))
     scale = np.abs(out[0]).max()
-    assert np.abs(out[1] - out[0]).max() <= 1e-6 * scale, np.abs(out[1] - out[0]).max() / scale
+    assert np.abs(out[1] - out[0]).max() <= TOL_DERIV[adj] * scale, np.abs(out[1] - out[0]).max() / scale
 
 
 @pytest.mark.parametrize("mode", ["fast", "exact"])

@@ -127,3 +127,35 @@ def test_multi_matches_single_instances(built_lib):
     vfull[: 3 * len(w["xv0"])] = gw.warpDerivFwd(tan[:nwp], solverVec=False)
     vfull[3 * (len(w["xv0"]) + len(bg)):] = gs.warpDerivFwd(tan[nwp:], solverVec=False)
     np.testing.assert_allclose(dv, vfull[ind], rtol=0, atol=1e-11 * np.abs(vfull).max())
+
+
+def test_constructor_from_plot3d_file(monkeypatch, tmp_path):
+    # MultiUSMesh(gridFile, optionsDict): a multi-block PLOT3D combined grid
+    # with cgns_utils-style block names; blocks of one zone form one group
+    import idwarp_gb300.MultiUnstructuredMesh as MM
+    from idwarp_gb300 import Error
+    from idwarp_gb300.plot3d import writePlot3D
+
+    monkeypatch.setattr(MM, "USMesh", _FakeMesh)
+    w, s, bg = _parts()
+    half = len(s["xv0"]) // 2
+    blocks = [w["xv0"], bg, s["xv0"][:half], s["xv0"][half:]]
+    sizes = [[len(b), 1, 1] for b in blocks]
+    f = tmp_path / "combined.xyz"
+    writePlot3D(str(f), np.concatenate(blocks), sizes)
+    names = ["wing.00000", "background.00000", "sphere.00000", "sphere.00001"]
+    with pytest.raises(Error, match="block names"):
+        MM.MultiUSMesh(str(f), {"wing": {}})
+    (tmp_path / "combined.xyz.names").write_text("\n".join(names) + "\n")
+    mm = MM.MultiUSMesh(str(f), {"wing": {}, "sphere": {}})
+    assert mm.names == ["wing", "sphere"]
+    assert mm.cgnsBlockIntervals == [[0, 1], [2, 4]]
+    nw, nb = 3 * len(w["xv0"]), bg.size
+    assert mm.cgnsVolNodeIntervals == [[0, nw], [nw + nb, nw + nb + s["xv0"].size]]
+    np.testing.assert_array_equal(mm.meshes[1].x, s["xv0"].ravel())
+    np.testing.assert_array_equal(mm.backgroundNodes[0], bg.ravel())
+    # explicit names win over the file; scattered blocks of a zone are refused
+    mm2 = MM.MultiUSMesh(f, {"wing": {}}, blockNames=["wing.0", "wing.1", "bg.0", "bg.1"])
+    assert mm2.cgnsBlockIntervals == [[0, 2]]
+    with pytest.raises(Error, match="not consecutive"):
+        MM.MultiUSMesh(str(f), {"wing": {}}, blockNames=["wing.0", "bg.0", "wing.1", "bg.1"])
