@@ -523,9 +523,19 @@ def run_suite_d(steps=50, sample=200000, directions=5):
                 "gradient_check_rotations": out["gradient_check"]})
     coef = torch.tensor(out["coef"], device="cuda")
     res["coef_max_abs"] = float(coef.abs().max())
-    # FD at the deformed state (rotations on), starting the check there
+    # FD at the deformed state (rotations on), starting the check there, with
+    # the differences of the FP64 form (the mixed forward's rounding is of the
+    # order of a 1e-6 step's effect)
+    o64 = mesh_options(m, "fp64")
+    with contextlib.redirect_stdout(io.StringIO()):
+        g64 = USMesh(options=o64)
+        g64.createCommonGrid(m["xv0"])
+        g64.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
+    chk = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions, coef0=coef, fd_mesh=g64)
+    res["gradient_check_rotations_deformed_fd64"] = chk["gradient_check"]
     chk = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions, coef0=coef)
     res["gradient_check_rotations_deformed"] = chk["gradient_check"]
+    del g64
     g.setOption("useRotations", False)
     out2 = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions)
     res["gradient_check_no_rotations"] = out2["gradient_check"]

@@ -854,7 +854,8 @@ int idw_warp_mesh_cs(void *ctx) {
     if (rc) return rc;
     c->haveWarp = true;
     // imaginary part: complex nodal properties, their cluster means, and
-    // the FP64 walk over (Im M + I, Im b) divided by the real denominator
+    // the FP64 walk in tangent mode over (Im M, Im b) divided by the real
+    // denominator
     const int n = c->nUnique;
     CKA(c->xuC.alloc(3 * size_t(n)));
     CKA(c->ptMBim.alloc(12 * size_t(n)));
@@ -938,6 +939,12 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
         c->batchCap = kBatchWalk;
     }
     SurfaceDev s = surf_dev(c);
+    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
+    // exact mode on a mesh that fills the GPU runs the tiled kernel once per
+    // surface (no decisions to share), on surface-major arrays; the batched
+    // walk reads point-major ones
+    const bool tiledExact = exact && c->nLeaves > 0 && c->opt.exactSchedule != IDW_EXACT_WALK &&
+                            (c->opt.exactSchedule == IDW_EXACT_TILED || exact_tiled_fills(c->nVol));
     if (tangent) launch_gather_xu(n, c->xuInd.p, c->xs.p, c->xu.p, c->stream);
     for (int b = 0; b < nb; ++b) {
         double *xu = c->bXu.p + size_t(b) * 3 * n, *mb = c->bPtMB.p + size_t(b) * 12 * n;
@@ -950,10 +957,19 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
             launch_nodal(s, xu, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p, c->opt.useRotations, mb,
                          c->stream);
         launch_set_data(tree_dev(c), mb, nmb, setdata_scratch(c), c->stream);
-        launch_mixed_nodal(n, tree_dev(c), nmb, c->ptXA.p, mb, c->bPtDM.p + size_t(b) * 12 * n,
-                           c->bPtDMl.p + size_t(b) * 12 * n, c->stream);
-        launch_mixed_nodes(tree_dev(c), nmb, mb, c->bNodeDC.p + size_t(b) * 12 * nn, c->bNodeDCl.p + size_t(b) * 12 * nn,
-                           c->bNodeDn.p + size_t(b) * nn, c->bRef.p + 24 * b, c->stream);
+        if (tiledExact) {
+            launch_mixed_nodal(n, tree_dev(c), nmb, c->ptXA.p, mb, c->bPtDM.p + size_t(b) * 12 * n,
+                               c->bPtDMl.p + size_t(b) * 12 * n, c->stream);
+            launch_mixed_nodes(tree_dev(c), nmb, mb, c->bNodeDC.p + size_t(b) * 12 * nn,
+                               c->bNodeDCl.p + size_t(b) * 12 * nn, c->bNodeDn.p + size_t(b) * nn, c->bRef.p + 24 * b,
+                               c->stream);
+        } else {
+            const int B = kBatchWalk;
+            launch_mixed_nodal(n, tree_dev(c), nmb, c->ptXA.p, mb, c->bPtDM.p + 12 * b, c->bPtDMl.p + 12 * b,
+                               c->stream, 12 * B);
+            launch_mixed_nodes(tree_dev(c), nmb, mb, c->bNodeDC.p + 12 * b, c->bNodeDCl.p + 12 * b, c->bNodeDn.p + b,
+                               c->bRef.p + 24 * b, c->stream, 12 * B, B);
+        }
     }
     int rc = check_launch(c, "batch nodal properties");
     if (rc) return rc;
@@ -964,7 +980,6 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
     k.slotStats = 0;
     k.exactSchedule = c->opt.exactSchedule;
     k.precGate = tangent ? tangentGate : mixed_gate(c);
-    const int exact = c->opt.evalMode == IDW_EVAL_EXACT;
     const TreeDevF tf = tree_devf(c);
     PointsDevF pf;
     pf.da = c->ptDA.p;
@@ -979,12 +994,23 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
     WalkRecF rec;
     rec.hi = c->recHi.p;
     rec.lo = c->recLo.p;
-    rc = ensure_gate_den(c, tf, pf, af, rec, k, exact);
-    if (rc) return rc;
+    {
+        // the gate's denominators depend on the weights only: the
+        // single-surface walk on the context's own arrays gives them
+        PointsDevF p1 = pf;
+        p1.dm = c->ptDM.p;
+        p1.dml = c->ptDMl.p;
+        NodeAggF a1 = af;
+        a1.dc = c->nodeDC.p;
+        a1.dcl = c->nodeDCl.p;
+        a1.dn = c->nodeDn.p;
+        a1.ref = c->refDB.p;
+        rc = ensure_gate_den(c, tf, p1, a1, rec, k, exact);
+        if (rc) return rc;
+    }
     rec.gden = c->gden.p;
     CK(cudaEventRecord(c->ev0, c->stream));
-    if (exact && tf.nLeaves > 0 && k.exactSchedule != IDW_EXACT_WALK &&
-        (k.exactSchedule == IDW_EXACT_TILED || exact_tiled_fills(c->nVol))) {
+    if (tiledExact) {
         // exact mode on a mesh that fills the GPU: the tiled kernel per surface
         // (no decisions to share between surfaces)
         const MixedParams mp = make_mixed_params(k);
@@ -1001,8 +1027,8 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
                                c->counters.p, c->stream);
         }
     } else {
-        launch_walk_mixed_batch(nb, tree_dev(c), tf, pf, 12 * int64_t(n), af, 12 * int64_t(nn), int64_t(nn),
-                                vol_dev(c), rec, k, exact, c->bAcc.p, 2 * c->nVol, c->counters.p, c->stream);
+        launch_walk_mixed_batch(nb, tree_dev(c), tf, pf, af, vol_dev(c), rec, k, exact, c->bAcc.p, 2 * c->nVol,
+                                c->counters.p, c->stream);
     }
     for (int b = 0; b < nb; ++b)
         launch_finalize_mixed(vol_dev(c), rec, c->bAcc.p + size_t(b) * 2 * c->nVol, k.law.bExp,
@@ -1397,9 +1423,10 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
     // Xu, Xud = Xs, Xsd at the first caller occurrence of each unique point
     launch_gather_xu(n, c->xuInd.p, c->xs.p, c->xu.p, c->stream);
     launch_gather_xu(n, c->xuInd.p, xsdDev, xud.p, c->stream);
-    // (Md + I, bd): the forward walk with S = (Md + I) r + bd - r = Md r + bd
+    // (Md, bd) for the FP64 walk in tangent mode (S = Md r + bd); (Md + I, bd)
+    // for the mixed walk, whose motions are relative to the identity
     launch_nodal_d(surf_dev(c), c->xu.p, xud.p, c->ptXA.p, c->normals0.p, c->tmpAi.p, c->isCorner.p,
-                   c->opt.useRotations, 1, ptMBd.p, c->stream);
+                   c->opt.useRotations, mixed ? 1 : 0, ptMBd.p, c->stream);
     launch_set_data(tree_dev(c), ptMBd.p, nodeMBd.p, setdata_scratch(c), c->stream);
     int rc = check_launch(c, "tangent nodal properties");
     if (rc) return rc;

@@ -5,6 +5,10 @@
 // motions S_b = M_b r + b_b - r differ per surface.  Each surface's result
 // equals that of the single-surface walk (idw_mixed.cu) up to rounding.
 //
+// The surfaces' point and cluster arrays are point-major (all surfaces of a
+// point, or of a cluster, in adjacent 48-byte rows), so a point's motions for
+// every surface come from one or two cache lines.
+//
 // Per lane: the denominator pair in registers; per surface the running
 // numerator pairs in shared memory.  Terms are summed in FP32 partials of at
 // most a leaf, or at most kFlush cluster terms, which are then added to the
@@ -45,9 +49,8 @@ __device__ __forceinline__ void flush_partials(BatchSmem<NB> &sm, float (&pn)[NB
 
 template <int KIND, int NB>
 __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
-    k_walk_mixed_batch(TreeDev t, TreeDevF tf, PointsDevF pf, int64_t ptStrideB, NodeAggF af, int64_t nodeStrideB,
-                       int64_t dnStrideB, VolumeDev v, WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
-                       float4 *acc, int64_t accStrideB, unsigned long long *counters) {
+    k_walk_mixed_batch(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af, VolumeDev v, WalkRecF rec, MixedParams mp,
+                       Law32<KIND> law, int exact, float4 *acc, int64_t accStrideB, unsigned long long *counters) {
     extern __shared__ __align__(16) unsigned char smraw[];
     BatchSmem<NB> &sm = *reinterpret_cast<BatchSmem<NB> *>(smraw);
     const int tid = threadIdx.x;
@@ -123,7 +126,7 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                         const float w = da.w * law.eval(tt, c1, ab, abl);
 #pragma unroll
                         for (int b = 0; b < NB; ++b) {
-                            const float4 *dm = reinterpret_cast<const float4 *>(pf.dm + b * ptStrideB + 12 * i);
+                            const float4 *dm = reinterpret_cast<const float4 *>(pf.dm + 12 * (kBatchMax * int64_t(i) + b));
                             const float4 m0 = ldgf4(dm), m1 = ldgf4(dm + 1), m2 = ldgf4(dm + 2);
                             pn[b][0] = fmaf(w, fmaf(m0.x, dx, fmaf(m0.y, dy, fmaf(m0.z, dz, m2.y))), pn[b][0]);
                             pn[b][1] = fmaf(w, fmaf(m0.w, dx, fmaf(m1.x, dy, fmaf(m1.y, dz, m2.z))), pn[b][1]);
@@ -137,7 +140,7 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
 #pragma unroll
                     for (int b = 0; b < NB; ++b)
                         lmag = fmaxf(lmag, fabsf(pn[b][0]) + fabsf(pn[b][1]) + fabsf(pn[b][2]) +
-                                               pd * __ldg(af.dn + b * dnStrideB + node) * hsum);
+                                               pd * __ldg(af.dn + kBatchMax * int64_t(node) + b) * hsum);
                     leafPrecise = KIND != 2 && lmag > gv;
                     if (!leafPrecise) {
                         flush_partials<NB>(sm, pn);
@@ -175,8 +178,8 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                             for (int b = 0; b < NB; ++b) {
                                 float s3[3] = {sm.sn[b][0][tid], sm.sn[b][1][tid], sm.sn[b][2][tid]};
                                 float c3[3] = {sm.cn[b][0][tid], sm.cn[b][1][tid], sm.cn[b][2][tid]};
-                                precise_motion(x, wh, wl, pf.dm + b * ptStrideB + 12 * i,
-                                               pf.dml + b * ptStrideB + 12 * i, s3, c3);
+                                precise_motion(x, wh, wl, pf.dm + 12 * (kBatchMax * int64_t(i) + b),
+                                               pf.dml + 12 * (kBatchMax * int64_t(i) + b), s3, c3);
 #pragma unroll
                                 for (int a = 0; a < 3; ++a) {
                                     sm.sn[b][a][tid] = s3[a];
@@ -207,13 +210,13 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                     float mag = 0.f;
 #pragma unroll
                     for (int b = 0; b < NB; ++b) {
-                        const float4 *dc = reinterpret_cast<const float4 *>(af.dc + b * nodeStrideB + 12 * node);
+                        const float4 *dc = reinterpret_cast<const float4 *>(af.dc + 12 * (kBatchMax * int64_t(node) + b));
                         const float4 m0 = ldgf4(dc), m1 = ldgf4(dc + 1), m2 = ldgf4(dc + 2);
                         S[b][0] = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
                         S[b][1] = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
                         S[b][2] = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
                         mag = fmaxf(mag, fabsf(S[b][0]) + fabsf(S[b][1]) + fabsf(S[b][2]) +
-                                             __ldg(af.dn + b * dnStrideB + node) * rsum);
+                                             __ldg(af.dn + kBatchMax * int64_t(node) + b) * rsum);
                     }
                     precise = KIND != 2 && w * mag > gv;
                     if (!precise) {
@@ -254,8 +257,8 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                         for (int b = 0; b < NB; ++b) {
                             float s3[3] = {sm.sn[b][0][tid], sm.sn[b][1][tid], sm.sn[b][2][tid]};
                             float c3[3] = {sm.cn[b][0][tid], sm.cn[b][1][tid], sm.cn[b][2][tid]};
-                            precise_motion(x, wh, wl, af.dc + b * nodeStrideB + 12 * node,
-                                           af.dcl + b * nodeStrideB + 12 * node, s3, c3);
+                            precise_motion(x, wh, wl, af.dc + 12 * (kBatchMax * int64_t(node) + b),
+                                           af.dcl + 12 * (kBatchMax * int64_t(node) + b), s3, c3);
 #pragma unroll
                             for (int a = 0; a < 3; ++a) {
                                 sm.sn[b][a][tid] = s3[a];
@@ -320,66 +323,55 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
 }
 
 template <int KIND, int NB>
-void launch_batch_nb(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, int64_t ptStrideB,
-                     const NodeAggF &af, int64_t nodeStrideB, int64_t dnStrideB, const VolumeDev &v,
-                     const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law, int exact, float4 *acc,
-                     int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
+void launch_batch_nb(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                     const VolumeDev &v, const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law, int exact,
+                     float4 *acc, int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
     const size_t smem = sizeof(BatchSmem<NB>);
     cudaFuncSetAttribute(k_walk_mixed_batch<KIND, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     const int g = int((v.nVol + 127) / 128);
-    k_walk_mixed_batch<KIND, NB><<<g, 128, smem, st>>>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp,
-                                                       law, exact, acc, accStrideB, counters);
+    k_walk_mixed_batch<KIND, NB><<<g, 128, smem, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB,
+                                                       counters);
 }
 
 template <int KIND>
-void launch_batch_kind(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, int64_t ptStrideB,
-                       const NodeAggF &af, int64_t nodeStrideB, int64_t dnStrideB, const VolumeDev &v,
-                       const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law, int exact, float4 *acc,
-                       int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
+void launch_batch_kind(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                       const VolumeDev &v, const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law,
+                       int exact, float4 *acc, int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
     switch (nb) {
         case 1:
-            launch_batch_nb<KIND, 1>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                                     accStrideB, counters, st);
+            launch_batch_nb<KIND, 1>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
             break;
         case 2:
-            launch_batch_nb<KIND, 2>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                                     accStrideB, counters, st);
+            launch_batch_nb<KIND, 2>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
             break;
         case 3:
-            launch_batch_nb<KIND, 3>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                                     accStrideB, counters, st);
+            launch_batch_nb<KIND, 3>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
             break;
         case 4:
-            launch_batch_nb<KIND, 4>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                                     accStrideB, counters, st);
+            launch_batch_nb<KIND, 4>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
             break;
         default:
-            launch_batch_nb<KIND, kBatchMax>(t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact,
-                                             acc, accStrideB, counters, st);
+            launch_batch_nb<KIND, kBatchMax>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
             break;
     }
 }
 
 }  // namespace
 
-void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, int64_t ptStrideB,
-                             const NodeAggF &af, int64_t nodeStrideB, int64_t dnStrideB, const VolumeDev &v,
-                             const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc, int64_t accStrideB,
-                             unsigned long long *counters, cudaStream_t st) {
+void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                             const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
+                             int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
     if (v.nVol <= 0 || nb <= 0) return;
     const MixedParams mp = make_mixed_params(k);
     if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         Law32<0> law{3, 5, 3.f, 5.f};
-        launch_batch_kind<0>(nb, t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                             accStrideB, counters, st);
+        launch_batch_kind<0>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
     } else if (k.law.isInt) {
         Law32<1> law{k.law.ia, k.law.ib, float(k.law.aExp), float(k.law.bExp)};
-        launch_batch_kind<1>(nb, t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                             accStrideB, counters, st);
+        launch_batch_kind<1>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
     } else {
         Law32<2> law{0, 0, float(k.law.aExp), float(k.law.bExp)};
-        launch_batch_kind<2>(nb, t, tf, pf, ptStrideB, af, nodeStrideB, dnStrideB, v, rec, mp, law, exact, acc,
-                             accStrideB, counters, st);
+        launch_batch_kind<2>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
     }
 }
 

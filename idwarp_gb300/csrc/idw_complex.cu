@@ -8,9 +8,9 @@
 //   Xv = Xv0 + sum w (M r + b - r) / sum w,   M, b complex,
 // whose real part is the ordinary warp of X and whose imaginary part is
 //   sum w (Im M r + Im b) / sum w,
-// the same walk applied to (Im M, Im b) (as a tangent walk, with the
-// identity added to Im M so that the walk's S = M r + b - r gives Im M r +
-// Im b).  This file computes M and b in complex arithmetic from the complex
+// the same walk applied to (Im M, Im b) as a tangent walk (motions M r + b:
+// an imaginary part of 1e-40 next to the identity, as in M r + b - r, would
+// round away).  This file computes M and b in complex arithmetic from the complex
 // coordinates (computeNodalProperties, kd_tree.F90:1580-1664) with the
 // templated geometry of idw_nodal_math.cuh; the walk is the FP64 one.
 #include "idw_common.cuh"
@@ -30,8 +30,8 @@ __global__ void k_gather_xu_cs(int n, const int *xuInd, const double *xsC, cplx 
     for (int a = 0; a < 3; ++a) xu[3 * i + a] = cplx(xsC[2 * (3 * j + a)], xsC[2 * (3 * j + a) + 1]);
 }
 
-// M_i, b_i in complex arithmetic; writes the imaginary parts, with the
-// identity added to Im M (tangent-walk form), 12 doubles per node.
+// M_i, b_i in complex arithmetic; writes their imaginary parts, 12 doubles
+// per node.
 __global__ void k_nodal_cs(SurfaceDev s, const cplx *Xu, const dbl4 *xa, const double *normals0, const double *Ai,
                            const int *isCorner, int useRotations, double *ptMBim) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,7 +51,7 @@ __global__ void k_nodal_cs(SurfaceDev s, const cplx *Xu, const dbl4 *xa, const d
     }
     double *o = ptMBim + 12 * i;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) o[k] = M[k].im + ((k % 4 == 0) ? 1.0 : 0.0);
+    for (int k = 0; k < 9; ++k) o[k] = M[k].im;
     o[9] = b[0].im;
     o[10] = b[1].im;
     o[11] = b[2].im;

@@ -163,10 +163,13 @@ void launch_dry_run(const TreeDev &t, const VolumeDev &v, const SymPlanes &sym, 
 int volume_bbox(int64_t n, const double *x, double *lo, double *hi, int64_t *nonFinite, cudaStream_t st);
 void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, const double *hi,
                          unsigned long long *codes, int *idx, cudaStream_t st);
+// pStride / nStride: floats between consecutive points / nodes of ptDM and
+// nodeDC (12 for one surface; 12 kBatchMax for the batched walk's
+// point-major arrays); dnStride likewise for nodeDn.
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
-                        float *ptDM, float *ptDMl, cudaStream_t st);
+                        float *ptDM, float *ptDMl, cudaStream_t st, int pStride = 12);
 void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
-                        float *nodeDn, float *refDB, cudaStream_t st);
+                        float *nodeDn, float *refDB, cudaStream_t st, int nStride = 12, int dnStride = 1);
 
 // Evaluation (idw_walk.cu)
 void launch_walk_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const double *nodeMB,
@@ -202,13 +205,14 @@ MixedParams make_mixed_params(const EvalConsts &k);
 #define IDW_BATCH_MAX 4
 #endif
 constexpr int kBatchMax = IDW_BATCH_MAX;
-// nb (1..kBatchMax) surfaces in one mixed walk (idw_batch.cu): per-surface point and
-// cluster arrays at strides ptStrideB / nodeStrideB / dnStrideB (floats), the
-// reference motions at af.ref + 24 b, accumulators at acc + accStrideB * b.
-void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, int64_t ptStrideB,
-                             const NodeAggF &af, int64_t nodeStrideB, int64_t dnStrideB, const VolumeDev &v,
-                             const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc, int64_t accStrideB,
-                             unsigned long long *counters, cudaStream_t st);
+// nb (1..kBatchMax) surfaces in one mixed walk (idw_batch.cu).  The point and
+// cluster arrays are point-major: surface b's 12 floats of point i at
+// pf.dm + 12 (kBatchMax i + b) (likewise dml, af.dc, af.dcl by node), its
+// bound at af.dn[kBatchMax q + b]; the reference motions at af.ref + 24 b,
+// accumulators at acc + accStrideB * b.
+void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                             const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
+                             int64_t accStrideB, unsigned long long *counters, cudaStream_t st);
 void launch_finalize_mixed(const VolumeDev &v, const WalkRecF &rec, const float4 *acc, double bExp, double *xv,
                            cudaStream_t st, int tangent = 0);
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,

@@ -296,15 +296,15 @@ __device__ __forceinline__ void split_store(double v, float *hi, float *lo) {
 // Per point: D' = M - I - Dref and u' = S'(Xu0) = (M - I) Xu0 + b - Dref Xu0 - bref,
 // FP32 high and low parts.
 __global__ void k_mixed_nodal(int n, TreeDev t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
-                              float *ptDM, float *ptDMl) {
+                              float *ptDM, float *ptDMl, int pStride) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double Dr[9], br[3];
     ref_motion(t, nodeMB, Dr, br);
     const double *m = ptMB + 12 * i;
     dbl4 x = ptXA[i];
-    float *o = ptDM + 12 * i;
-    float *ol = ptDMl + 12 * i;
+    float *o = ptDM + int64_t(pStride) * i;
+    float *ol = ptDMl + int64_t(pStride) * i;
     double X[3] = {x.x, x.y, x.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -326,7 +326,7 @@ __global__ void k_mixed_nodal(int n, TreeDev t, const double *nodeMB, const dbl4
 // walk's precision gate.  Thread 0 also stores the reference motion (Dref 9,
 // bref 3; high parts then low parts) that the walk adds back.
 __global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
-                              float *nodeDn, float *refDB) {
+                              float *nodeDn, float *refDB, int nStride, int dnStride) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= t.nNodes) return;
     double Dr[9], br[3];
@@ -346,14 +346,14 @@ __global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, const double *ptM
                 dn = fmax(dn, rs);
             }
         }
-        nodeDn[q] = float(dn);
+        nodeDn[int64_t(dnStride) * q] = float(dn);
         return;
     }
     const double *m = nodeMB + 12 * q;
     dbl4 g = t.geom[q];
     double X[3] = {g.x, g.y, g.z};
-    float *o = nodeDC + 12 * q;
-    float *ol = nodeDCl + 12 * q;
+    float *o = nodeDC + int64_t(nStride) * q;
+    float *ol = nodeDCl + int64_t(nStride) * q;
     double dn = 0.0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -368,7 +368,7 @@ __global__ void k_mixed_nodes(TreeDev t, const double *nodeMB, const double *ptM
         dn = fmax(dn, rowsum);
         split_store(Mx + (m[9 + a] - br[a]), o + 9 + a, ol + 9 + a);
     }
-    nodeDn[q] = float(dn);
+    nodeDn[int64_t(dnStride) * q] = float(dn);
 }
 
 
@@ -478,15 +478,16 @@ void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, cons
 
 
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
-                        float *ptDM, float *ptDMl, cudaStream_t st) {
+                        float *ptDM, float *ptDMl, cudaStream_t st, int pStride) {
     if (n > 0 && t.nNodes > 0)
-        k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, t, nodeMB, ptXA, ptMB, ptDM, ptDMl);
+        k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, t, nodeMB, ptXA, ptMB, ptDM, ptDMl, pStride);
 }
 
 void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
-                        float *nodeDn, float *refDB, cudaStream_t st) {
+                        float *nodeDn, float *refDB, cudaStream_t st, int nStride, int dnStride) {
     if (t.nNodes > 0)
-        k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, ptMB, nodeDC, nodeDCl, nodeDn, refDB);
+        k_mixed_nodes<<<blocks(t.nNodes, 256), 256, 0, st>>>(t, nodeMB, ptMB, nodeDC, nodeDCl, nodeDn, refDB, nStride,
+                                                              dnStride);
 }
 
 // Sort volume nodes by Morton code (set-up).  perm[k] = common index of the

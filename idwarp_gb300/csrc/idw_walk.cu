@@ -50,15 +50,18 @@ __device__ __forceinline__ void load12(const double *src, double *d) {
     }
 }
 
-// One exact pair (kd_tree.F90:677-688).
+// One exact pair (kd_tree.F90:677-688).  tangent: the pair's motion is
+// M r + b (the tangent's Md r + bd, warpDerivFwd.F90), without the - r of
+// the warp's M r + b - r.
 __device__ __forceinline__ void pair64(const EvalConsts &k, const dbl4 &x, const double *mb, const double *r,
-                                       double *num, double &den) {
+                                       int tangent, double *num, double &den) {
     double r0 = r[0] - x.x, r1 = r[1] - x.y, r2 = r[2] - x.z;
     double LoD = k.law.Ldef / sqrt(r0 * r0 + r1 * r1 + r2 * r2 + 1e-15);
     double W = x.w * law64(k.law, LoD);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        double S = mb[3 * a] * r[0] + mb[3 * a + 1] * r[1] + mb[3 * a + 2] * r[2] + mb[9 + a] - r[a];
+        double S = mb[3 * a] * r[0] + mb[3 * a + 1] * r[1] + mb[3 * a + 2] * r[2] + mb[9 + a];
+        if (!tangent) S -= r[a];
         num[a] += W * S;
     }
     den += W;
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(128) k_walk64(TreeDev t, PointsDev p, VolumeDe
             for (int i = 0; i < nPts; ++i) {
                 double mb[12];
                 load12(p.mb + 12 * i, mb);
-                pair64(k, ldg4(p.xa + i), mb, r, num, den);
+                pair64(k, ldg4(p.xa + i), mb, r, o.tangent, num, den);
             }
             cnt.leafPairs += valid ? nPts : 0;
             cnt.visited += valid ? 1 : 0;
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(128) k_walk64(TreeDev t, PointsDev p, VolumeDe
                         for (int i = inf.x; i <= inf.y; ++i) {
                             double mb[12];
                             load12(p.mb + 12 * i, mb);
-                            pair64(k, ldg4(p.xa + i), mb, r, num, den);
+                            pair64(k, ldg4(p.xa + i), mb, r, o.tangent, num, den);
                         }
                         cnt.leafPairs += inf.y - inf.x + 1;
                         cnt.visited++;
@@ -114,8 +117,8 @@ __global__ void __launch_bounds__(128) k_walk64(TreeDev t, PointsDev p, VolumeDe
                             load12(nodeMB + 12 * node, mb);
 #pragma unroll
                             for (int a = 0; a < 3; ++a) {
-                                double S = mb[3 * a] * r[0] + mb[3 * a + 1] * r[1] + mb[3 * a + 2] * r[2] + mb[9 + a] -
-                                           r[a];
+                                double S = mb[3 * a] * r[0] + mb[3 * a + 1] * r[1] + mb[3 * a + 2] * r[2] + mb[9 + a];
+                                if (!o.tangent) S -= r[a];
                                 num[a] += W * S;
                             }
                             den += W;

@@ -72,13 +72,15 @@ def inverse_volume_objective(xv, cells, eps):
 
 
 def ffd_loop(mesh, xs0, cells, ffd, steps=50, lr=1e-3, eps=1e-12, check_directions=5, fd_step=1e-6, seed=300,
-             coef0=None):
+             coef0=None, fd_mesh=None):
     """Gradient steps (Adam) on the FFD coefficients minimising
     sum(1 / max(V_cell, eps)) of the warped grid, from ``coef0`` (zero by
     default: the undeformed surface).  Before the loop the gradient is
     checked against central differences on ``check_directions`` random
-    directions.  Returns a dict with the objective history, the gradient
-    check and timings."""
+    directions; the differences are taken with ``fd_mesh`` when given (an
+    FP64 mesh of the same grid: a step of 1e-6 is below the resolution of
+    the mixed forward's own rounding), else with ``mesh``.  Returns a dict
+    with the objective history, the gradient check and timings."""
     dev = xs0.device
     B, sel = ffd.torch_operator(dev)
     if coef0 is None:
@@ -86,8 +88,10 @@ def ffd_loop(mesh, xs0, cells, ffd, steps=50, lr=1e-3, eps=1e-12, check_directio
     else:
         coef = torch.as_tensor(coef0, dtype=torch.float64, device=dev).clone().requires_grad_(True)
 
-    def objective(c):
-        return inverse_volume_objective(warp(ffd.apply(xs0, c, B, sel), mesh), cells, eps)
+    def objective(c, m=mesh):
+        return inverse_volume_objective(warp(ffd.apply(xs0, c, B, sel), m), cells, eps)
+
+    fdm = fd_mesh if fd_mesh is not None else mesh
 
     f0 = objective(coef)
     f0.backward()
@@ -97,8 +101,8 @@ def ffd_loop(mesh, xs0, cells, ffd, steps=50, lr=1e-3, eps=1e-12, check_directio
     with torch.no_grad():
         for _ in range(check_directions):
             d = torch.tensor(rng.normal(size=ffd.nVars), device=dev)
-            fp = objective(coef + fd_step * d).item()
-            fm = objective(coef - fd_step * d).item()
+            fp = objective(coef + fd_step * d, fdm).item()
+            fm = objective(coef - fd_step * d, fdm).item()
             fd = (fp - fm) / (2 * fd_step)
             ad = float(torch.dot(g0, d))
             check.append({"ad": ad, "fd": fd, "rel": abs(ad - fd) / max(abs(fd), 1e-300)})
