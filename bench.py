@@ -533,6 +533,11 @@ def run_suite_d(steps=50, sample=200000, directions=5):
         g64.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
     chk = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions, coef0=coef, fd_mesh=g64)
     res["gradient_check_rotations_deformed_fd64"] = chk["gradient_check"]
+    # the same with the gradient of the FP64 form too (FP64 forward and
+    # adjoint): the derivative itself, without the mixed forward's rounding
+    # in the objective's 1/V of the wall cells
+    chk = ffd_loop(g64, xs0, cells, ffd, steps=0, check_directions=directions, coef0=coef)
+    res["gradient_check_rotations_deformed_fp64"] = chk["gradient_check"]
     chk = ffd_loop(g, xs0, cells, ffd, steps=0, check_directions=directions, coef0=coef)
     res["gradient_check_rotations_deformed"] = chk["gradient_check"]
     del g64
@@ -577,6 +582,45 @@ def run_suite_d(steps=50, sample=200000, directions=5):
     return 0
 
 
+def run_case(case, cfg, reps):
+    """One operation on a config's mesh, repeated: the small cases the ncu
+    captures profile (warp: warpMesh; deriv1: warpDeriv of one seed, double-float
+    form; deriv1fast: the FP32 form; batch: 8 surfaces through warpMeshBatch)."""
+    import torch
+
+    from idwarp_gb300 import _lib
+    from idwarp_gb300 import synthetic as S
+
+    m = make_workload(cfg)
+    mesh = build_mesh(m, "mixed")
+    L = mesh.lib
+    L.idw_set_stream(mesh.ctx, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    mesh.setSurfaceCoordinates(m["xs"])
+    mesh.warpMesh()
+    nvol = len(m["xv0"])
+    if case in ("deriv1", "deriv1fast"):
+        if case == "deriv1fast":
+            mesh.setOption("adjointPrecision", "fast")
+            mesh._setMeshOptions()
+        sd = torch.tensor(np.random.default_rng(100).normal(size=(nvol, 3)), device="cuda")
+        for _ in range(reps):
+            _lib.check(L, mesh.ctx, L.idw_warp_deriv(mesh.ctx, C.c_void_p(sd.data_ptr()), 3 * nvol, _lib.IDW_DEVICE),
+                       "warpDeriv")
+    elif case == "batch":
+        sb = torch.tensor(np.stack([S.wing_perturbation(m["pts"], seed=200 + i) for i in range(8)]), device="cuda")
+        ob = torch.empty((8, nvol, 3), dtype=torch.float64, device="cuda")
+        for _ in range(reps):
+            _lib.check(L, mesh.ctx, L.idw_warp_mesh_batch(mesh.ctx, C.c_void_p(sb.data_ptr()), 8,
+                                                          C.c_void_p(ob.data_ptr()), _lib.IDW_DEVICE),
+                       "warpMeshBatch")
+    else:
+        for _ in range(reps):
+            mesh.warpMesh()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": case, "config": cfg, "reps": reps, "lastKernelMs": mesh.getStats()["lastKernelMs"]}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -590,7 +634,14 @@ def main():
                     help="evalMode of the timed warp; the extra measurements and the CPU baseline are fast-mode only")
     ap.add_argument("--suite", action="store_true", help="measurement table rows (S1, W, P errTol sweep)")
     ap.add_argument("--suite-d", action="store_true", help="the 20M-node two-body FFD loop")
+    ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "batch"],
+                    help="run one operation --steps times on --config's mesh (the small profiling cases)")
     args = ap.parse_args()
+    if args.case:
+        import torch
+
+        torch.cuda.set_device(_env_int("LOCAL_RANK", 0))
+        return run_case(args.case, args.config, args.steps)
     if args.suite or args.suite_d:
         import torch
 
