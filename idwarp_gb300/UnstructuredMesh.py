@@ -277,17 +277,30 @@ class USMesh(BaseSolver):
                                                      _lib.IDW_HOST), "warp_to_solver_grid")
         return solverGrid
 
-    def getWarpGrid(self, out=None):
+    def getWarpGrid(self, out=None, wait=True):
         """Current grid in warp order, flat (3*nVol,).  ``out`` (optional) is a
         contiguous float64 host array of that size to fill, e.g. in pinned
-        memory for fast repeated reads."""
+        memory for fast repeated reads.  ``wait=False`` (with ``out``) queues
+        the copy and returns at once: ``out`` is complete after
+        ``synchronize()``, and the copy overlaps the work queued after it (the
+        next warpMesh writes another device buffer meanwhile)."""
         if out is None:
+            if not wait:
+                raise Error("getWarpGrid(wait=False) needs an output array (out=...).")
             out = np.zeros(3 * self.nVol, np.float64)
         elif out.dtype != np.float64 or out.size != 3 * self.nVol or not out.flags.c_contiguous:
             raise Error("getWarpGrid(out=...) needs a contiguous float64 array of %d entries." % (3 * self.nVol))
-        self._chk(self.lib.idw_get_volume_coordinates(self.ctx, C.c_void_p(out.ctypes.data), out.size,
-                                                        _lib.IDW_HOST), "getWarpGrid")
+        if wait:
+            self._chk(self.lib.idw_get_volume_coordinates(self.ctx, C.c_void_p(out.ctypes.data), out.size,
+                                                            _lib.IDW_HOST), "getWarpGrid")
+        else:
+            self._chk(self.lib.idw_get_volume_coordinates_async(self.ctx, C.c_void_p(out.ctypes.data), out.size),
+                      "getWarpGrid")
         return out
+
+    def synchronize(self):
+        """Wait for the mesh's queued GPU work and asynchronous grid reads."""
+        self._chk(self.lib.idw_synchronize(self.ctx), "synchronize")
 
     def getCommonGrid(self):
         """Grid in the original (common) ordering, flat (3*nVol,)."""

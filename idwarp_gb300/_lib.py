@@ -97,6 +97,7 @@ _SIGS = {
     "idw_warp_mesh_batch": [_VP, _VP, C.c_int32, _VP, C.c_int],
     "idw_get_volume_coordinates": [_VP, _VP, C.c_int64, C.c_int],
     "idw_get_common_volume_coordinates": [_VP, _VP, C.c_int64, C.c_int],
+    "idw_get_volume_coordinates_async": [_VP, _VP, C.c_int64],
     "idw_set_volume_coordinates": [_VP, _VP, C.c_int64, C.c_int],
     "idw_set_external_mesh_indices": [_VP, _IP, C.c_int64],
     "idw_get_solver_mesh_dof": [_VP, C.POINTER(C.c_int64)],

@@ -110,6 +110,18 @@ struct Ctx {
     // solver ordering
     DevBuf<int> solverInd;
     int64_t nSolver = -1;
+    // asynchronous reads of the warped grid (idw_get_volume_coordinates_async):
+    // a copy stream, the grid's second buffer, and per buffer the event that
+    // ends its last read (a warp writes the other buffer while a read of the
+    // current one may still run)
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evReady = nullptr;
+    DevBuf<double> xvAlt;
+    struct PendingRead {
+        const double *p = nullptr;
+        cudaEvent_t ev = nullptr;
+        bool on = false;
+    } rd[2];
     // misc
     DevBuf<unsigned long long> counters;
     bool eventsRecorded = false;
@@ -360,6 +372,13 @@ int idw_destroy(void *ctx) {
     if (!c) return IDW_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copyStream) {
+        cudaStreamSynchronize(c->copyStream);
+        cudaStreamDestroy(c->copyStream);
+    }
+    if (c->evReady) cudaEventDestroy(c->evReady);
+    for (auto &r : c->rd)
+        if (r.ev) cudaEventDestroy(r.ev);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     delete c;
@@ -384,6 +403,7 @@ int idw_synchronize(void *ctx) {
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     CK(cudaStreamSynchronize(c->stream));
+    if (c->copyStream) CK(cudaStreamSynchronize(c->copyStream));
     return IDW_OK;
 }
 
@@ -402,6 +422,13 @@ int idw_create_common_grid(void *ctx, const double *volnodes, int64_t nvol, int 
     if (!c) return IDW_ERR_ARG;
     if (nvol < 0 || nvol > (int64_t(1) << 31) - 1) return fail(c, IDW_ERR_ARG, "nvol out of range: %lld", (long long)nvol);
     CK(cudaSetDevice(c->device));
+    // a new grid: asynchronous reads of the old one end first
+    if (c->copyStream) CK(cudaStreamSynchronize(c->copyStream));
+    for (auto &r : c->rd) {
+        r.on = false;
+        r.p = nullptr;
+    }
+    c->xvAlt.release();
     c->nVol = nvol;
     CKA(c->xv0.alloc(3 * nvol));
     CKA(c->xv.alloc(3 * nvol));
@@ -739,6 +766,27 @@ static int ensure_gate_den(Ctx *c, const TreeDevF &tf, const PointsDevF &pf, con
     return IDW_OK;
 }
 
+// Before the warped grid is overwritten: if an asynchronous read of the
+// current grid may still run, the next grid goes to the other buffer; an
+// older read of that buffer (one warp back) is waited for on the stream.
+static int prepare_xv_write(Ctx *c) {
+    for (auto &r : c->rd) {
+        if (r.on && r.p == c->xv.p) {
+            CKA(c->xvAlt.alloc(c->xv.n));
+            std::swap(c->xv.p, c->xvAlt.p);
+            std::swap(c->xv.n, c->xvAlt.n);
+            break;
+        }
+    }
+    for (auto &r : c->rd) {
+        if (r.on && r.p == c->xv.p) {
+            CK(cudaStreamWaitEvent(c->stream, r.ev, 0));
+            r.on = false;
+        }
+    }
+    return IDW_OK;
+}
+
 static int run_warp(Ctx *c, double *xvOut, double *denOut) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
     if (int e0 = ensure_den0(c)) return e0;
@@ -813,7 +861,9 @@ int idw_warp_mesh(void *ctx) {
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     CK(cudaSetDevice(c->device));
-    int rc = run_warp(c, c->xv.p, c->den.p);
+    int rc = prepare_xv_write(c);
+    if (rc) return rc;
+    rc = run_warp(c, c->xv.p, c->den.p);
     if (rc) return rc;
     c->haveWarp = true;
     return IDW_OK;
@@ -849,8 +899,10 @@ int idw_warp_mesh_cs(void *ctx) {
     if (c->opt.precision != IDW_PREC_FP64) return fail(c, IDW_ERR_STATE, "the complex step runs in FP64 precision");
     if (!c->haveCs) return fail(c, IDW_ERR_STATE, "complex surface coordinates must be set first");
     CK(cudaSetDevice(c->device));
+    int rc = prepare_xv_write(c);
+    if (rc) return rc;
     // real part: the ordinary warp of the real coordinates (also sets den)
-    int rc = run_warp(c, c->xv.p, c->den.p);
+    rc = run_warp(c, c->xv.p, c->den.p);
     if (rc) return rc;
     c->haveWarp = true;
     // imaginary part: complex nodal properties, their cluster means, and
@@ -1112,12 +1164,43 @@ int idw_get_common_volume_coordinates(void *ctx, double *out, int64_t ndof, int 
     return idw_get_volume_coordinates(ctx, out, ndof, where);
 }
 
+int idw_get_volume_coordinates_async(void *ctx, double *out, int64_t ndof) {
+    Ctx *c = static_cast<Ctx *>(ctx);
+    if (!c) return IDW_ERR_ARG;
+    if (ndof != 3 * c->nVol) return fail(c, IDW_ERR_ARG, "ndof mismatch: %lld vs %lld", (long long)ndof, (long long)(3 * c->nVol));
+    if (ndof > 0 && !out) return fail(c, IDW_ERR_ARG, "null output pointer");
+    CK(cudaSetDevice(c->device));
+    if (!c->copyStream) {
+        CK(cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->evReady, cudaEventDisableTiming));
+        for (auto &r : c->rd) CK(cudaEventCreateWithFlags(&r.ev, cudaEventDisableTiming));
+    }
+    // the read of this buffer's slot (or the slot of the other buffer's older read)
+    Ctx::PendingRead *slot = nullptr;
+    for (auto &r : c->rd)
+        if (r.p == c->xv.p) slot = &r;
+    if (!slot)
+        for (auto &r : c->rd)
+            if (!r.on || r.p != c->xvAlt.p) slot = &r;
+    if (!slot) return fail(c, IDW_ERR_STATE, "no free read slot");
+    CK(cudaEventRecord(c->evReady, c->stream));
+    CK(cudaStreamWaitEvent(c->copyStream, c->evReady, 0));
+    if (ndof > 0)
+        CK(cudaMemcpyAsync(out, c->xv.p, sizeof(double) * size_t(ndof), cudaMemcpyDeviceToHost, c->copyStream));
+    CK(cudaEventRecord(slot->ev, c->copyStream));
+    slot->p = c->xv.p;
+    slot->on = true;
+    return IDW_OK;
+}
+
 int idw_set_volume_coordinates(void *ctx, const double *in, int64_t ndof, int where) {
     Ctx *c = static_cast<Ctx *>(ctx);
     if (!c) return IDW_ERR_ARG;
     if (ndof != 3 * c->nVol) return fail(c, IDW_ERR_ARG, "ndof mismatch");
     CK(cudaSetDevice(c->device));
-    int rc = copy_in(c, c->xv.p, in, size_t(ndof), where);
+    int rc = prepare_xv_write(c);
+    if (rc) return rc;
+    rc = copy_in(c, c->xv.p, in, size_t(ndof), where);
     if (rc) return rc;
     CK(cudaStreamSynchronize(c->stream));
     return IDW_OK;

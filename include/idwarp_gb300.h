@@ -120,7 +120,7 @@ int idw_last_error(void *ctx, char *buf, int len);
 
 /* Use `stream` (a cudaStream_t, NULL = default stream) for all later work. */
 int idw_set_stream(void *ctx, void *stream);
-int idw_synchronize(void *ctx);
+int idw_synchronize(void *ctx); /* also waits for asynchronous grid reads */
 
 /* Update options (UnstructuredMesh.py:1051-1069 _setMeshOptions).  As in the
  * reference, aExp/bExp/bucketSize/cornerAngle/zeroCornerRotations take effect
@@ -187,6 +187,14 @@ int idw_warp_mesh_batch(void *ctx, const double *coords, int32_t nbatch, double 
  * (getvolumecoordinates, libidwarp.pyf:45-48; getcommonvolumecoordinates
  * :50-53) */
 int idw_get_volume_coordinates(void *ctx, double *out, int64_t ndof, int where);
+/* idw_get_volume_coordinates into host memory without waiting: the copy is
+ * queued on a copy stream of the context behind the work queued so far and
+ * overlaps whatever is queued next (e.g. the next warp, which then writes a
+ * second device buffer).  out is complete after idw_synchronize; for the copy
+ * to run asynchronously it should be page-locked (cudaHostAlloc, torch
+ * pin_memory).  No reference counterpart (getvolumecoordinates,
+ * libidwarp.pyf:45-48, returns when the copy is done). */
+int idw_get_volume_coordinates_async(void *ctx, double *out, int64_t ndof);
 int idw_get_common_volume_coordinates(void *ctx, double *out, int64_t ndof, int where);
 /* (setvolumecoordinates, src/warp/getVolumeCoordinates.F90:25-46) */
 int idw_set_volume_coordinates(void *ctx, const double *in, int64_t ndof, int where);

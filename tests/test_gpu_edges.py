@@ -182,3 +182,36 @@ def test_plot3d_grid_file_roundtrip(tmp_path, built_lib):
     back, sz = readPlot3D(str(out), return_blocks=True)
     np.testing.assert_array_equal(sz, sizes)
     np.testing.assert_array_equal(back, g.getCommonGrid().reshape(-1, 3))
+
+
+def test_async_grid_reads(sphere, built_lib):
+    # getWarpGrid(wait=False): reads queued behind each warp, while the next
+    # warp writes the other device buffer; every read must hold its own warp
+    import torch
+
+    from idwarp_gb300 import synthetic as S
+
+    g = build_gpu(sphere, precision="mixed")
+    surfaces = [S.sphere_perturbation(sphere["pts"], seed=k) for k in range(5)]
+    want = []
+    for xs in surfaces:
+        g.setSurfaceCoordinates(xs)
+        g.warpMesh()
+        want.append(g.getWarpGrid().copy())
+    n = 3 * len(sphere["xv0"])
+    bufs = [torch.empty(n, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    got = []
+    for k, xs in enumerate(surfaces):
+        g.setSurfaceCoordinates(xs)
+        g.warpMesh()
+        g.getWarpGrid(out=bufs[k % 3], wait=False)
+        if k % 3 == 2:
+            g.synchronize()
+            got += [b.copy() for b in bufs]
+    g.synchronize()
+    got += [bufs[k % 3].copy() for k in range(len(got), len(surfaces))]
+    for k in range(len(surfaces)):
+        np.testing.assert_array_equal(got[k], want[k])
+    # the synchronous read still sees the latest warp
+    np.testing.assert_array_equal(g.getWarpGrid(), want[-1])
+
