@@ -28,12 +28,12 @@ namespace idw {
 
 namespace {
 
-constexpr int kPChunk = 8;  // leaf points reduced per shared-memory pass
-
 template <int S>
 struct PrecSmem {
     static constexpr int kC = S > 0 ? 3 * S : 1;
-    static constexpr int kP = S > 0 ? kPChunk : 1;
+    // leaf points reduced per shared-memory pass: a whole leaf of the default
+    // bucket (up to 9 points) in one pass for few seeds, 8 for 16 seeds
+    static constexpr int kP = S == 0 ? 1 : (S <= 4 ? 10 : 8);
     float nh[32][kC], nl[32][kC];      // seeds of every lane (numb, scaled), hi / lo
     float4 vh[kP][32], vl[kP][32];     // per term: w, w (r - C), hi / lo
 };
