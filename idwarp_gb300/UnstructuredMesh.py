@@ -103,6 +103,7 @@ class USMesh(BaseSolver):
             "diagnostics": [int, 0],
             "exactSchedule": [str, ["auto", "tiled", "walk"]],
             "adjointPrecision": [str, ["precise", "fast"]],
+            "walkLists": [str, ["auto", "off"]],
         }
 
     # ------------------------------------------------------------------
@@ -562,6 +563,7 @@ class USMesh(BaseSolver):
         o.diagnostics = self.getOption("diagnostics")
         o.exactSchedule = {"auto": 0, "tiled": 1, "walk": 2}[self.getOption("exactSchedule")]
         o.adjointPrecision = {"precise": _lib.IDW_ADJ_PRECISE, "fast": _lib.IDW_ADJ_FAST}[self.getOption("adjointPrecision")]
+        o.walkLists = {"auto": _lib.IDW_WALK_LISTS_AUTO, "off": _lib.IDW_WALK_LISTS_OFF}[self.getOption("walkLists")]
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

@@ -18,6 +18,8 @@ IDW_PREC_FP64 = 0
 IDW_PREC_MIXED = 1
 IDW_ADJ_PRECISE = 0
 IDW_ADJ_FAST = 1
+IDW_WALK_LISTS_AUTO = 0
+IDW_WALK_LISTS_OFF = 1
 IDW_OK = 0
 IDW_ERR_ARG = -1
 IDW_ERR_STATE = -2
@@ -40,7 +42,7 @@ class idw_options(C.Structure):
         ("evalMode", C.c_int32), ("useRotations", C.c_int32), ("zeroCornerRotations", C.c_int32),
         ("bucketSize", C.c_int32), ("precision", C.c_int32), ("diagnostics", C.c_int32),
         ("mixedGate", C.c_double), ("exactSchedule", C.c_int32), ("adjointPrecision", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("walkLists", C.c_int32), ("reserved", C.c_int32 * 1),
     ]
 
 

@@ -16,7 +16,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libidwarp_gb300.so")
 
-SOURCES = ["idw_api.cu", "idw_walk.cu", "idw_mixed.cu", "idw_batch.cu", "idw_exact.cu", "idw_adjoint.cu", "idw_adjoint_precise.cu", "idw_nodal.cu", "idw_setup.cu",
+SOURCES = ["idw_api.cu", "idw_walk.cu", "idw_mixed.cu", "idw_replay.cu", "idw_batch.cu", "idw_exact.cu", "idw_adjoint.cu", "idw_adjoint_precise.cu", "idw_nodal.cu", "idw_setup.cu",
            "idw_probe.cu", "idw_complex.cu", "idw_host.cpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -99,6 +99,15 @@ struct Ctx {
     double denPLdefFact = 0.0, denPAlpha = 0.0;
     int denPMode = -1;
     DevBuf<float> ptDM, ptDMl, nodeDC, nodeDCl, nodeDn, refDB;
+    // recorded decisions of the fast walk (idw_replay.cu), valid for the
+    // current den0 and listErrTol; listState 1 = recorded, -1 = too large
+    // (the walks decide as they go), 0 = not yet recorded
+    DevBuf<int64_t> walkOffs;
+    DevBuf<int2> walkList;
+    DevBuf<unsigned long long> walkCnt;
+    int listState = 0;
+    double listErrTol = 0.0;
+    int64_t listEntries = 0;
     // adjoint
     DevBuf<double> ptAdj, nodeAdj, xub, dxs;
     bool haveDxs = false;
@@ -264,6 +273,8 @@ int validate_options(Ctx *c, const idw_options *o) {
         return fail(c, IDW_ERR_ARG, "exactSchedule must be IDW_EXACT_AUTO, IDW_EXACT_TILED or IDW_EXACT_WALK");
     if (o->adjointPrecision != IDW_ADJ_PRECISE && o->adjointPrecision != IDW_ADJ_FAST)
         return fail(c, IDW_ERR_ARG, "adjointPrecision must be IDW_ADJ_PRECISE or IDW_ADJ_FAST");
+    if (o->walkLists != IDW_WALK_LISTS_AUTO && o->walkLists != IDW_WALK_LISTS_OFF)
+        return fail(c, IDW_ERR_ARG, "walkLists must be IDW_WALK_LISTS_AUTO or IDW_WALK_LISTS_OFF");
     return IDW_OK;
 }
 
@@ -291,6 +302,7 @@ int finish_den0(Ctx *c) {
     if (e) return e;
     c->gdenValid = false;
     c->denPValid = false;
+    c->listState = 0;
     c->den0Valid = true;
     return IDW_OK;
 }
@@ -333,6 +345,7 @@ void idw_default_options(idw_options *o) {
     o->diagnostics = 0;
     o->mixedGate = 2e-3;
     o->adjointPrecision = IDW_ADJ_PRECISE;
+    o->walkLists = IDW_WALK_LISTS_AUTO;
 }
 
 int idw_create(const idw_options *opts, void **ctx_out) {
@@ -459,6 +472,7 @@ int idw_create_common_grid(void *ctx, const double *volnodes, int64_t nvol, int 
     c->haveVolume = true;
     // a new volume needs a new initialize (records and estimates are per node)
     c->haveTree = false;
+    c->listState = 0;
     c->den0Valid = false;
     c->haveWarp = false;
     c->haveDxs = false;
@@ -696,6 +710,7 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     CKA(c->gden.alloc(size_t(c->nVol)));
     c->gdenValid = false;
     c->denPValid = false;
+    c->listState = 0;
     c->den0Valid = false;
     CK(cudaStreamSynchronize(st));
     c->haveTree = true;
@@ -741,6 +756,48 @@ int idw_get_surface_coordinates(void *ctx, double *coords, int64_t cdof, int whe
 // of FP32 terms.
 static double mixed_gate(const Ctx *c) {
     return c->opt.mixedGate * c->Ldef0 * std::min(1.0, 2.0 / double(std::max(1, c->sym.nLoop)));
+}
+
+// The fast walk's decisions depend on set-up state and errTol only: record
+// them once (count pass, offsets, record pass) and hand them to every later
+// mixed walk in k.lists.  The lists take up to half of the free device memory;
+// beyond that the walks keep deciding as they go.  Returns a status; k.lists
+// stays null when the lists are off or do not fit.
+static int ensure_walk_lists(Ctx *c, const TreeDevF &tf, const WalkRecF &rec, EvalConsts &k) {
+    k.lists = WalkLists{};
+    if (c->opt.precision != IDW_PREC_MIXED || c->opt.evalMode != IDW_EVAL_FAST ||
+        c->opt.walkLists == IDW_WALK_LISTS_OFF || c->nVol <= 0 || k.slotStats)
+        return IDW_OK;
+    if (c->listState != 0 && c->listErrTol != c->opt.errTol) c->listState = 0;
+    if (c->listState == 0) {
+        c->walkList.release();
+        const int64_t nOff = walk_list_warps(c->nVol) * c->sym.nLoop + 1;
+        CKA(c->walkOffs.alloc(size_t(nOff)));
+        CKA(c->walkCnt.alloc(8));
+        const int64_t total = count_walk_lists(tree_dev(c), tf, vol_dev(c), rec, k, c->walkOffs.p, c->stream);
+        if (total < 0) return fail(c, IDW_ERR_CUDA, "walk lists: count pass failed");
+        size_t freeB = 0, totalB = 0;
+        CK(cudaMemGetInfo(&freeB, &totalB));
+        c->listErrTol = c->opt.errTol;
+        c->listEntries = total;
+        if (double(total) * sizeof(int2) > 0.5 * double(freeB)) {
+            c->listState = -1;
+            return IDW_OK;
+        }
+        CKA(c->walkList.alloc(size_t(std::max<int64_t>(total, 1))));
+        CK(cudaMemsetAsync(c->walkCnt.p, 0, 8 * sizeof(unsigned long long), c->stream));
+        launch_walk_record(tree_dev(c), tf, vol_dev(c), rec, k, c->walkOffs.p, c->walkList.p, c->walkCnt.p,
+                           c->stream);
+        int rc = check_launch(c, "walk lists");
+        if (rc) return rc;
+        c->listState = 1;
+    }
+    if (c->listState == 1) {
+        k.lists.offs = c->walkOffs.p;
+        k.lists.list = c->walkList.p;
+        k.lists.counters = c->walkCnt.p;
+    }
+    return IDW_OK;
 }
 
 // The mixed walk's precision gate wants each node's final denominator, which
@@ -825,7 +882,9 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
-        int rc2 = ensure_gate_den(c, tf, pf, af, rec, k, exact);
+        int rc2 = ensure_walk_lists(c, tf, rec, k);
+        if (rc2) return rc2;
+        rc2 = ensure_gate_den(c, tf, pf, af, rec, k, exact);
         if (rc2) return rc2;
         rec.gden = c->gden.p;
         CK(cudaEventRecord(c->ev0, c->stream));
@@ -1558,6 +1617,11 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
         rec.gden = c->gdenValid ? c->gden.p : nullptr;
+        if (c->listState == 1 && c->listErrTol == c->opt.errTol && !exact) {
+            k.lists.offs = c->walkOffs.p;
+            k.lists.list = c->walkList.p;
+            k.lists.counters = c->walkCnt.p;
+        }
         CK(cudaEventRecord(c->ev0, c->stream));
         launch_walk_mixed(tree_dev(c), tf, pf, af, vol_dev(c), rec, k, exact, c->acc.p, o, c->stream);
     } else {

@@ -110,6 +110,15 @@ struct WalkOut {
     const double *denIn = nullptr;
 };
 
+// Recorded decisions of the mixed fast walk (idw_replay.cu): per warp of 32
+// volume nodes and mirror, the tree nodes where some lane approximates or sums
+// a leaf, with the lane mask; null when the walks decide as they go.
+struct WalkLists {
+    const int64_t *offs = nullptr;   // warps x nLoop + 1 entry offsets
+    const int2 *list = nullptr;      // entries {node | 0x80000000 for a leaf, lane mask}
+    const unsigned long long *counters = nullptr;  // the recording walk's leafPairs, approx, visited, fp64Fallback
+};
+
 struct EvalConsts {
     WeightLaw law;
     double errTol;
@@ -117,6 +126,7 @@ struct EvalConsts {
     int slotStats;
     double precGate;  // mixed walk: weight x lever-arm threshold for double-float cluster terms
     int exactSchedule = 0;  // IDW_EXACT_AUTO / _TILED / _WALK (mixed exact mode)
+    WalkLists lists;        // fast mode: replay these decisions when set
 };
 
 // Nodal properties (idw_nodal.cu)
@@ -179,6 +189,19 @@ void launch_walk_records(const VolumeDev &v, const SymPlanes &sym, double bExp, 
 void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
                        const VolumeDev &v, const WalkRecF &rec, const EvalConsts &k, int exact, float4 *acc,
                        const WalkOut &o, cudaStream_t st);
+// Recorded decisions (idw_replay.cu).  count_walk_lists fills offs (warps x
+// nLoop + 1) and returns the number of entries (-1 on a CUDA error; it
+// synchronises st); launch_walk_record writes them and the walk's counters;
+// launch_walk_replay evaluates the forward sums from k.lists into acc.
+int64_t walk_list_warps(int64_t nVol);
+int64_t count_walk_lists(const TreeDev &t, const TreeDevF &tf, const VolumeDev &v, const WalkRecF &rec,
+                         const EvalConsts &k, int64_t *offs, cudaStream_t st);
+void launch_walk_record(const TreeDev &t, const TreeDevF &tf, const VolumeDev &v, const WalkRecF &rec,
+                        const EvalConsts &k, const int64_t *offs, int2 *list, unsigned long long *counters,
+                        cudaStream_t st);
+void launch_walk_replay(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, const VolumeDev &v,
+                        const WalkRecF &rec, const EvalConsts &k, float4 *acc, unsigned long long *counters,
+                        cudaStream_t st);
 // Exact mode as a tiled N-body kernel (idw_exact.cu); launch_walk_mixed uses
 // it for exact = 1.  Fills acc like the walk; no finalisation.
 void launch_exact_mixed(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, const VolumeDev &v,

@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
     mirS[threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
     mirC[threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
     MixedCounters cnt;
+    const WalkLane<KIND> wl = {law, Ls, LsLo, c1, ab, abl, gv};
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
         const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
@@ -62,45 +63,13 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
             if (STATS && __any_sync(kFull, active) && counters && (threadIdx.x & 31) == 0)
                 atomicAdd(counters + (inf.w ? 4 : 5), (unsigned long long)(inf.w ? 32 * (inf.y - inf.x + 1) : 32));
             if (inf.w) {
-                bool leafPrecise = false;
+                leaf_step<KIND>(active, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, sn, cn, sd, cd, counters);
                 if (active) {
-                    const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
-                    // r - C as hi + lo: exact high parts, so a volume node on a
-                    // surface node resolves d^2 = eps (1e-15) to full precision
-                    float h0, h1, h2, l0, l1, l2;
-                    two_diff(rh[0], ch.x, h0, l0);
-                    two_diff(rh[1], ch.y, h1, l1);
-                    two_diff(rh[2], ch.z, h2, l2);
-                    l0 += rl[0] - cl.x;
-                    l1 += rl[1] - cl.y;
-                    l2 += rl[2] - cl.z;
-                    float pn0 = 0.f, pn1 = 0.f, pn2 = 0.f, pd = 0.f;
-                    for (int i = inf.x; i <= inf.y; ++i) {
-                        const float4 *dm = reinterpret_cast<const float4 *>(pf.dm + 12 * i);
-                        leaf_pair<KIND>(law, Ls, LsLo, c1, ab, abl, h0, h1, h2, l0, l1, l2, ldgf4(pf.da + i),
-                                        ldgf4(pf.dl + i), ldgf4(dm), ldgf4(dm + 1), ldgf4(dm + 2), pn0, pn1, pn2, pd);
-                    }
-                    // a leaf carrying a large weight at a long lever arm is
-                    // re-summed in double-float (same gate as cluster terms)
-                    leafPrecise = leaf_close<KIND>(pn0, pn1, pn2, pd, __ldg(af.dn + node), h0, h1, h2, gv, sn, cn, sd,
-                                                   cd);
                     cnt.leafPairs += inf.y - inf.x + 1;
                     cnt.visited++;
                 }
-                if (__any_sync(kFull, leafPrecise)) {
-                    if (leafPrecise) {
-                        RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
-                        a = precise_leaf_ool<KIND>(a, tf, pf, node, inf.x, inf.y, rh[0], rh[1], rh[2], rl[0], rl[1],
-                                                   rl[2], law, Ls, LsLo, c1, mp.abH, mp.abL);
-                        sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
-                        cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
-                        sd = a.sd, cd = a.cd;
-                    }
-                    warp_count(counters, 6, leafPrecise ? unsigned(inf.y - inf.x + 1) : 0u);
-                }
                 node = inf.z;
             } else {
-                bool open = false;
                 int dec = 0;  // 0 open, 1 approximate, 2 undecided in FP32
                 float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
                 if (active && !exact) {
@@ -108,43 +77,14 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                     dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
                 }
                 dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
-                bool precise = false;
+                approx_step<KIND>(dec == 1, tf, af, node, rho0, rho1, rho2, rs, wA, rh, rl, wl, sn, cn, sd, cd,
+                                  counters);
+                bool open = false;
                 if (dec == 1) {
-                    const float tt = fmaf(Ls, rs, LsLo * rs);
-                    const float w = wA * law.eval(tt, c1, ab, abl);
-                    const float4 *dc = reinterpret_cast<const float4 *>(af.dc + 12 * node);
-                    const float4 m0 = ldgf4(dc), m1 = ldgf4(dc + 1), m2 = ldgf4(dc + 2);
-                    const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
-                    const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
-                    const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
-                    // a far cluster with a large weight at a long lever arm is
-                    // re-evaluated in double-float below
-                    const float mag = fabsf(S0) + fabsf(S1) + fabsf(S2) +
-                                      __ldg(af.dn + node) * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
-                    precise = KIND != 2 && w * mag > gv;
-                    if (!precise) {
-                        kahan_add(sn[0], cn[0], w * S0);
-                        kahan_add(sn[1], cn[1], w * S1);
-                        kahan_add(sn[2], cn[2], w * S2);
-                        kahan_add(sd, cd, w);
-                    }
                     skip = inf.z;
                     cnt.approx++;
                 } else if (active) {
                     open = true;
-                }
-                if (__any_sync(kFull, precise)) {
-                    if (precise) {
-                        RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
-                        a = precise_cluster<KIND>(a, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2],
-                                                  ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo),
-                                                  __ldg(&tf.nodes[node].aLo), af.dc + 12 * node, af.dcl + 12 * node,
-                                                  law, Ls, LsLo, c1, mp.abH, mp.abL);
-                        sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
-                        cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
-                        sd = a.sd, cd = a.cd;
-                    }
-                    warp_count(counters, 6, precise ? 1u : 0u);
                 }
                 node = __any_sync(kFull, open) ? node + 1 : inf.z;
             }
@@ -288,6 +228,13 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
         (k.exactSchedule == IDW_EXACT_TILED || exact_tiled_fills(v.nVol))) {
         // every pair: the tiled kernel, with the walk's arithmetic
         launch_exact_mixed(tf, pf, af, v, rec, mp, k.law, acc, o.counters, st);
+    } else if (!exact && k.lists.list && !mp.slotStats) {
+        // recorded decisions: the walk's terms without the walk's decisions;
+        // the work counters are the recording walk's
+        if (o.counters && k.lists.counters)
+            cudaMemcpyAsync(o.counters, k.lists.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                            st);
+        launch_walk_replay(tf, pf, af, v, rec, k, acc, o.counters, st);
     } else if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         launch_walk_kind(g, t, tf, pf, af, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, acc, o.counters, st);
     } else if (k.law.isInt) {

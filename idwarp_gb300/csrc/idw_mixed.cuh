@@ -287,9 +287,12 @@ __device__ __forceinline__ void precise_term(const dfl xin[3], float eps, float 
 // (open), 1 (approximate) or 2 (too close to a threshold for FP32: the caller
 // re-takes it with decide64).  Also returns r - C (FP32), |r - C|^2, its
 // reciprocal square root and the node area, which the approximation needs.
-__device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const float *rh, const float *rl, float tauf,
-                                        float &rho0, float &rho1, float &rho2, float &d2, float &rs, float &wA) {
-    const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+// The geometry of a cluster term from the split point (rh + rl) and the split
+// centroid (ch + cl; cl.w is the node area): r - C in FP32, |r - C|^2 and its
+// reciprocal square root.  Shared by the decision and by every walk that
+// evaluates the term, so a replayed term is bitwise the walked one.
+__device__ __forceinline__ void cluster_geo(const float4 ch, const float4 cl, const float *rh, const float *rl,
+                                            float &rho0, float &rho1, float &rho2, float &d2, float &rs, float &wA) {
     wA = cl.w;
     rho0 = (rh[0] - ch.x) + (rl[0] - cl.x);
     rho1 = (rh[1] - ch.y) + (rl[1] - cl.y);
@@ -299,6 +302,12 @@ __device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const floa
     // FP64) or far above the subnormal range (the components are differences
     // of hi/lo splits, resolved to ~1e-15), so the flush-to-zero form serves
     rs = rsqrt_normal(d2);
+}
+
+__device__ __forceinline__ int decide32(const TreeDevF &tf, int node, const float *rh, const float *rl, float tauf,
+                                        float &rho0, float &rho1, float &rho2, float &d2, float &rs, float &wA) {
+    const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+    cluster_geo(ch, cl, rh, rl, rho0, rho1, rho2, d2, rs, wA);
     const float dOvrR = d2 * rs * ch.w;
     if (dOvrR < 2.0f * (1.0f - 4e-6f)) return 0;
     if (dOvrR <= 2.0f * (1.0f + 4e-6f)) return 2;
@@ -518,6 +527,103 @@ __device__ __noinline__ RunSums precise_leaf_ool(RunSums a, const TreeDevF tf, c
     const float rh[3] = {rh0, rh1, rh2}, rl[3] = {rl0, rl1, rl2};
     precise_leaf<KIND>(tf, pf, node, lo, hi, rh, rl, law, Ls, LsLo, c1, abH, abL, a.sn, a.cn, a.sd, a.cd);
     return a;
+}
+
+// ---- the two kinds of walk step, shared by the decision walk (idw_mixed.cu)
+// and the replay of recorded decisions (idw_replay.cu), so both sum the same
+// terms with the same arithmetic in the same order ----
+
+// Per-lane constants of a forward mixed walk.
+template <int KIND>
+struct WalkLane {
+    Law32<KIND> law;
+    float Ls, LsLo, c1, ab, abl, gv;
+};
+
+// A leaf summed by the lanes with `mine` set: pair terms relative to the leaf
+// centroid, partial sums into the running pairs, and heavy leaves (the gate of
+// leaf_close) re-summed in double-float.  Called by all 32 lanes.
+template <int KIND>
+__device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
+                                          int node, int lo, int hi, const float *rh, const float *rl,
+                                          const WalkLane<KIND> &wl, float *sn, float *cn, float &sd, float &cd,
+                                          unsigned long long *counters) {
+    bool leafPrecise = false;
+    if (mine) {
+        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+        // r - C as hi + lo: exact high parts, so a volume node on a surface
+        // node resolves d^2 = eps (1e-15) to full precision
+        float h0, h1, h2, l0, l1, l2;
+        two_diff(rh[0], ch.x, h0, l0);
+        two_diff(rh[1], ch.y, h1, l1);
+        two_diff(rh[2], ch.z, h2, l2);
+        l0 += rl[0] - cl.x;
+        l1 += rl[1] - cl.y;
+        l2 += rl[2] - cl.z;
+        float pn0 = 0.f, pn1 = 0.f, pn2 = 0.f, pd = 0.f;
+        for (int i = lo; i <= hi; ++i) {
+            const float4 *dm = reinterpret_cast<const float4 *>(pf.dm + 12 * i);
+            leaf_pair<KIND>(wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl, h0, h1, h2, l0, l1, l2, ldgf4(pf.da + i),
+                            ldgf4(pf.dl + i), ldgf4(dm), ldgf4(dm + 1), ldgf4(dm + 2), pn0, pn1, pn2, pd);
+        }
+        // a leaf carrying a large weight at a long lever arm is re-summed in
+        // double-float (same gate as cluster terms)
+        leafPrecise = leaf_close<KIND>(pn0, pn1, pn2, pd, __ldg(af.dn + node), h0, h1, h2, wl.gv, sn, cn, sd, cd);
+    }
+    if (__any_sync(kFull, leafPrecise)) {
+        if (leafPrecise) {
+            RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
+            a = precise_leaf_ool<KIND>(a, tf, pf, node, lo, hi, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2], wl.law,
+                                       wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl);
+            sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
+            cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
+            sd = a.sd, cd = a.cd;
+        }
+        warp_count(counters, 6, leafPrecise ? unsigned(hi - lo + 1) : 0u);
+    }
+}
+
+// A cluster approximated by the lanes with `mine` set, from its geometry
+// (cluster_geo): w = A law(L/d), S = D' (r - C) + c'; terms with a large weight
+// at a long lever arm are re-evaluated in double-float.  Called by all 32 lanes.
+template <int KIND>
+__device__ __forceinline__ void approx_step(bool mine, const TreeDevF &tf, const NodeAggF &af, int node, float rho0,
+                                            float rho1, float rho2, float rs, float wA, const float *rh,
+                                            const float *rl, const WalkLane<KIND> &wl, float *sn, float *cn,
+                                            float &sd, float &cd, unsigned long long *counters) {
+    bool precise = false;
+    if (mine) {
+        const float tt = fmaf(wl.Ls, rs, wl.LsLo * rs);
+        const float w = wA * wl.law.eval(tt, wl.c1, wl.ab, wl.abl);
+        const float4 *dc = reinterpret_cast<const float4 *>(af.dc + 12 * node);
+        const float4 m0 = ldgf4(dc), m1 = ldgf4(dc + 1), m2 = ldgf4(dc + 2);
+        const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
+        const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
+        const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
+        // a far cluster with a large weight at a long lever arm is
+        // re-evaluated in double-float below
+        const float mag = fabsf(S0) + fabsf(S1) + fabsf(S2) +
+                          __ldg(af.dn + node) * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
+        precise = KIND != 2 && w * mag > wl.gv;
+        if (!precise) {
+            kahan_add(sn[0], cn[0], w * S0);
+            kahan_add(sn[1], cn[1], w * S1);
+            kahan_add(sn[2], cn[2], w * S2);
+            kahan_add(sd, cd, w);
+        }
+    }
+    if (__any_sync(kFull, precise)) {
+        if (precise) {
+            RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
+            a = precise_cluster<KIND>(a, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2], ldgf4(&tf.nodes[node].cHi),
+                                      ldgf4(&tf.nodes[node].cLo), __ldg(&tf.nodes[node].aLo), af.dc + 12 * node,
+                                      af.dcl + 12 * node, wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl);
+            sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
+            cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
+            sd = a.sd, cd = a.cd;
+        }
+        warp_count(counters, 6, precise ? 1u : 0u);
+    }
 }
 
 // End of one mirror pass: add the reference motion back, num += den (Dref r +

@@ -56,6 +56,10 @@ extern "C" {
 #define IDW_ADJ_PRECISE 0 /* mixed warpDeriv in double-float (FP32 pairs): terms, products and lane sums */
 #define IDW_ADJ_FAST 1    /* mixed warpDeriv with FP32 weights, products and lane sums */
 
+#define IDW_WALK_LISTS_AUTO 0 /* mixed fast mode: record the walk's decisions once and replay them
+                               * (when the lists fit in half of the free device memory) */
+#define IDW_WALK_LISTS_OFF 1  /* every walk takes its decisions as it goes */
+
 /* Mesh options: the gridinput module variables (src/modules/gridInput.f90:9-18,
  * libidwarp.pyf:148-162) plus kd_tree.bucket_size (libidwarp.pyf:204-206) and
  * the GB300 precision switch.  Semantics follow doc/options.yaml. */
@@ -84,7 +88,12 @@ typedef struct idw_options {
     int32_t adjointPrecision; /* mixed warpDeriv: IDW_ADJ_PRECISE (default) or
                                * IDW_ADJ_FAST (FP32 terms, a few 1e-7 relative per
                                * term; real-valued exponents always use FP32) */
-    int32_t reserved[2];
+    int32_t walkLists;    /* IDW_WALK_LISTS_AUTO (default) or IDW_WALK_LISTS_OFF: the fast
+                           * walk's open/approximate decisions depend on the set-up state
+                           * and errTol only, so they can be recorded once (per warp of 32
+                           * volume nodes: the tree nodes where a lane approximates or sums
+                           * a leaf) and replayed by every later warp; same sums either way */
+    int32_t reserved[1];
 } idw_options;
 
 /* Work counters of the last warp / warpDeriv call. */
