@@ -55,10 +55,13 @@ def make_workload(cfg, seed=2):
     return m
 
 
+WALK_LISTS = "auto"  # --walk-lists: "off" makes every walk decide as it goes
+
+
 def mesh_options(m, precision, mode="fast"):
     return {"fileType": "NPY", "precision": precision, "evalMode": mode, "errTol": ERR_TOL,
             "aExp": 3.0, "bExp": 5.0, "LdefFact": 1.0, "alpha": 0.25, "bucketSize": 8,
-            "symmetryPlanes": m["symmetryPlanes"]}
+            "symmetryPlanes": m["symmetryPlanes"], "walkLists": WALK_LISTS}
 
 
 def build_mesh(m, precision, mode="fast", restartFile=None):
@@ -585,7 +588,8 @@ def run_suite_d(steps=50, sample=200000, directions=5):
 def run_case(case, cfg, reps):
     """One operation on a config's mesh, repeated: the small cases the ncu
     captures profile (warp: warpMesh; deriv1: warpDeriv of one seed, double-float
-    form; deriv1fast: the FP32 form; batch: 8 surfaces through warpMeshBatch)."""
+    form; deriv1fast: the FP32 form; deriv16 / deriv16fast: 16 seeds in one
+    call; batch: 8 surfaces through warpMeshBatch)."""
     import torch
 
     from idwarp_gb300 import _lib
@@ -598,14 +602,21 @@ def run_case(case, cfg, reps):
     mesh.setSurfaceCoordinates(m["xs"])
     mesh.warpMesh()
     nvol = len(m["xv0"])
-    if case in ("deriv1", "deriv1fast"):
-        if case == "deriv1fast":
+    if case.startswith("deriv"):
+        if case.endswith("fast"):
             mesh.setOption("adjointPrecision", "fast")
             mesh._setMeshOptions()
-        sd = torch.tensor(np.random.default_rng(100).normal(size=(nvol, 3)), device="cuda")
+        ns = 16 if case.startswith("deriv16") else 1
+        sd = torch.tensor(np.random.default_rng(100).normal(size=(ns, nvol, 3)), device="cuda")
+        npts = len(m["xs"])
+        out = torch.zeros((ns, npts, 3), dtype=torch.float64, device="cuda")
         for _ in range(reps):
-            _lib.check(L, mesh.ctx, L.idw_warp_deriv(mesh.ctx, C.c_void_p(sd.data_ptr()), 3 * nvol, _lib.IDW_DEVICE),
-                       "warpDeriv")
+            if ns == 1:
+                rc = L.idw_warp_deriv(mesh.ctx, C.c_void_p(sd.data_ptr()), 3 * nvol, _lib.IDW_DEVICE)
+            else:
+                rc = L.idw_warp_deriv_batch(mesh.ctx, C.c_void_p(sd.data_ptr()), ns, C.c_void_p(out.data_ptr()),
+                                            _lib.IDW_DEVICE)
+            _lib.check(L, mesh.ctx, rc, "warpDeriv")
     elif case == "batch":
         sb = torch.tensor(np.stack([S.wing_perturbation(m["pts"], seed=200 + i) for i in range(8)]), device="cuda")
         ob = torch.empty((8, nvol, 3), dtype=torch.float64, device="cuda")
@@ -634,9 +645,13 @@ def main():
                     help="evalMode of the timed warp; the extra measurements and the CPU baseline are fast-mode only")
     ap.add_argument("--suite", action="store_true", help="measurement table rows (S1, W, P errTol sweep)")
     ap.add_argument("--suite-d", action="store_true", help="the 20M-node two-body FFD loop")
-    ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "batch"],
+    ap.add_argument("--walk-lists", default="auto", choices=["auto", "off"],
+                    help="mixed fast mode: replay recorded walk decisions (auto) or decide in every walk (off)")
+    ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "deriv16", "deriv16fast", "batch"],
                     help="run one operation --steps times on --config's mesh (the small profiling cases)")
     args = ap.parse_args()
+    global WALK_LISTS
+    WALK_LISTS = args.walk_lists
     if args.case:
         import torch
 
@@ -736,7 +751,14 @@ def main():
         if rc != 0:
             _lib.check(L, mesh.ctx, rc, "warpMesh")
 
-    for _ in range(args.warmup):
+    # the first warp records the walk's decisions (walk lists) and the
+    # precision gate's denominators: set-up work, timed apart from the steps
+    barrier()
+    t_first = time.perf_counter()
+    step()
+    barrier()
+    first_warp_s = time.perf_counter() - t_first
+    for _ in range(max(0, args.warmup - 1)):
         step()
     barrier()
     clocks = ClockSampler(local_rank)
@@ -793,9 +815,12 @@ def main():
                 "max_diff_between_step_outputs": e2e_check},
         "clocks": clk,
         # per step: gather_xu, face_props, nodal, set_data, mixed_nodal,
-        # mixed_nodes, walk, finalize
-        "gpu_launches": 8 * args.steps,
+        # mixed_nodes, walk, finalize (+ the replay's counter add)
+        "gpu_launches": (9 if st["walkListEntries"] > 0 else 8) * args.steps,
         "setup_s": setup_s,
+        "first_warp_s": first_warp_s,
+        "walk_lists": {"entries": st["walkListEntries"], "bytes": 8 * max(0, st["walkListEntries"]),
+                       "note": "decisions recorded by the first warp (first_warp_s) and replayed by every step"},
         "work": {"leafPairs": st["leafPairs"], "approx": st["approx"], "visited": st["visited"],
                  "fp64Fallback": st["fp64Fallback"]},
     }
@@ -803,12 +828,14 @@ def main():
     flops = 42.0 * (st["leafPairs"] + st["approx"])
     peak = fp32_peak_tflops() if not args.no_extras else None
     achieved = flops / (kernel_ms * 1e-3) / 1e12 if kernel_ms > 0 else None
-    # DRAM traffic of the walk: ncu dram__bytes_read.sum + dram__bytes_write.sum of
-    # k_walk_mixed on the 2M-node wing (148.4 + 42.0 MB for 2,025,050 volume
-    # nodes), scaled by volume nodes: the traffic is the per-node records and
-    # accumulators, the tree stays in L2
-    traffic = 94.0 * nvol
-    walk_kernel = "k_exact_mixed" if args.mode == "exact" else "k_walk_mixed"
+    # DRAM traffic of the walk: ncu dram__bytes_read.sum + dram__bytes_write.sum
+    # on the 2M-node wing (2,025,050 volume nodes), scaled by volume nodes: the
+    # per-node records, accumulators and (replay) the warps' decision lists;
+    # the tree stays in L2.  k_walk_mixed: 148.4 + 42.0 MB; k_walk_replay:
+    # 269.3 + 50.4 MB
+    replay = args.mode == "fast" and st["walkListEntries"] > 0
+    traffic = (157.9 if replay else 94.0) * nvol
+    walk_kernel = "k_exact_mixed" if args.mode == "exact" else ("k_walk_replay" if replay else "k_walk_mixed")
     out["roofline"] = {"bound": "fp32", "kernel": walk_kernel, "achieved": achieved, "unit": "TFLOP/s",
                        "peak": peak, "peak_source": "measured FFMA probe (idw_probe_ffma) in this run",
                        "frac": (achieved / peak) if (achieved and peak) else None,

@@ -52,7 +52,7 @@ class idw_stats(C.Structure):
         ("nUnique", C.c_int64), ("nTreeNodes", C.c_int64), ("maxDepth", C.c_int64), ("nVol", C.c_int64),
         ("nSurfPts", C.c_int64), ("nLoop", C.c_int64), ("Ldef0", C.c_double), ("lastKernelMs", C.c_double),
         ("warpLeafSlots", C.c_int64), ("warpNodeSlots", C.c_int64), ("preciseTerms", C.c_int64),
-        ("reserved", C.c_int64 * 1),
+        ("walkListEntries", C.c_int64),
     ]
 
     def as_dict(self):

@@ -166,12 +166,14 @@ __device__ __forceinline__ void reduce_one_s1(const float4 v, const float n[3], 
     warp_land_moments(P, d);
 }
 
-template <int S, int KIND>
+// REPLAY: walk the recorded decisions (idw_replay.cu) instead of deciding.
+template <int S, int KIND, int REPLAY>
 __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, VolumeDev v,
                                                        WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
                                                        const double *dxv, int64_t dxvStride, const double *den,
                                                        double *ptAdj, int64_t ptStride, double *nodeAdj,
-                                                       int64_t nodeStride, unsigned long long *counters) {
+                                                       int64_t nodeStride, unsigned long long *counters,
+                                                       WalkLists wlists) {
     extern __shared__ __align__(16) unsigned char smraw[];
     AdjSmem<S> &sm = reinterpret_cast<AdjSmem<S> *>(smraw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -225,9 +227,22 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
         }
         __syncwarp();
         int node = 0, skip = 0;
-        while (node < t.nNodes) {
+        int64_t e = 0, e1 = 0;
+        if (REPLAY && (gid >> 5) < (v.nVol + 31) / 32) {
+            e = wlists.offs[(gid >> 5) * mp.nLoop + kk];
+            e1 = wlists.offs[(gid >> 5) * mp.nLoop + kk + 1];
+        }
+        while (REPLAY ? e < e1 : node < t.nNodes) {
+            bool active;
+            if (REPLAY) {
+                const int2 ent = __ldg(wlists.list + e);
+                ++e;
+                node = ent.x & 0x7fffffff;
+                active = (unsigned(ent.y) >> lane) & 1u;
+            } else {
+                active = valid && node >= skip;
+            }
             const int4 inf = ldgi4(&tf.nodes[node].info);
-            const bool active = valid && node >= skip;
             if (inf.w) {
                 if (__any_sync(kFull, active)) {
                     float h0 = 0.f, h1 = 0.f, h2 = 0.f, l0 = 0.f, l1 = 0.f, l2 = 0.f;
@@ -264,16 +279,24 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                             reduce_terms<S>(sm, m, targets, ptAdj, ptStride);
                     }
                 }
-                node = inf.z;
+                if (!REPLAY) node = inf.z;
             } else {
                 bool open = false;
                 int dec = 0;
                 float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
-                if (active && !exact) {
-                    cnt.visited++;
-                    dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                if (REPLAY) {
+                    if (active) {
+                        cluster_geo(ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo), rh, rl, rho0, rho1, rho2,
+                                    d2, rs, wA);
+                        dec = 1;
+                    }
+                } else {
+                    if (active && !exact) {
+                        cnt.visited++;
+                        dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                    }
+                    dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 }
-                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 if (__any_sync(kFull, dec == 1)) {
                     float w = 0.f;
                     if (dec == 1) {
@@ -294,13 +317,15 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         }
                     }
                 }
-                if (dec != 1 && active) open = true;
-                node = __any_sync(kFull, open) ? node + 1 : inf.z;
+                if (!REPLAY) {
+                    if (dec != 1 && active) open = true;
+                    node = __any_sync(kFull, open) ? node + 1 : inf.z;
+                }
             }
         }
         __syncwarp();
     }
-    cnt.flush(counters);
+    if (!REPLAY) cnt.flush(counters);
 }
 
 // Combine the point and cluster moments into the relative adjoints the
@@ -351,28 +376,35 @@ template <int S, int KIND>
 void launch_adj(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
                 const MixedParams &mp, const Law32<KIND> &law, int exact, const double *dxv, int64_t dxvStride,
                 const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj, int64_t nodeStride,
-                unsigned long long *counters, cudaStream_t st) {
+                unsigned long long *counters, const WalkLists &wl, cudaStream_t st) {
     const size_t smem = 4 * sizeof(AdjSmem<S>);
-    cudaFuncSetAttribute(k_adjoint_mixed<S, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     const int g = int((v.nVol + 127) / 128);
-    k_adjoint_mixed<S, KIND><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den, ptAdj,
-                                                   ptStride, nodeAdj, nodeStride, counters);
+    if (wl.list && !exact) {
+        launch_add_walk_counters(counters, wl.counters, st);
+        cudaFuncSetAttribute(k_adjoint_mixed<S, KIND, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        k_adjoint_mixed<S, KIND, 1><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den,
+                                                          ptAdj, ptStride, nodeAdj, nodeStride, counters, wl);
+    } else {
+        cudaFuncSetAttribute(k_adjoint_mixed<S, KIND, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        k_adjoint_mixed<S, KIND, 0><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den,
+                                                          ptAdj, ptStride, nodeAdj, nodeStride, counters, wl);
+    }
 }
 
 template <int S>
 void launch_adj_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                     const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, int exact, const double *dxv,
                     int64_t dxvStride, const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj,
-                    int64_t nodeStride, unsigned long long *counters, cudaStream_t st) {
+                    int64_t nodeStride, unsigned long long *counters, const WalkLists &lists, cudaStream_t st) {
     if (wl.isInt && wl.ia == 3 && wl.ib == 5) {
         launch_adj<S, 0>(t, tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, dxv, dxvStride, den, ptAdj, ptStride,
-                         nodeAdj, nodeStride, counters, st);
+                         nodeAdj, nodeStride, counters, lists, st);
     } else if (wl.isInt) {
         launch_adj<S, 1>(t, tf, pf, v, rec, mp, Law32<1>{wl.ia, wl.ib, float(wl.aExp), float(wl.bExp)}, exact, dxv,
-                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, st);
+                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, lists, st);
     } else {
         launch_adj<S, 2>(t, tf, pf, v, rec, mp, Law32<2>{0, 0, float(wl.aExp), float(wl.bExp)}, exact, dxv,
-                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, st);
+                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, lists, st);
     }
 }
 
@@ -408,22 +440,22 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
         // seeds in groups of 16, 8, 4 or 1 sharing one walk, none above maxGroup
         if (left >= 16 && maxGroup >= 16) {
             launch_adj_law<16>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                               counters, st);
+                               counters, k.lists, st);
             s0 += 16;
         } else if (left >= 8 && maxGroup >= 8) {
             launch_adj_law<8>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                              counters, st);
+                              counters, k.lists, st);
             s0 += 8;
         } else if (left >= 4 && maxGroup >= 4) {
             launch_adj_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                              counters, st);
+                              counters, k.lists, st);
             s0 += 4;
         } else if (tiledOne) {
             launch_exact_adjoint(tf, pf, v, rec, mp, k.law, d, den, pa, counters, st);
             s0 += 1;
         } else {
             launch_adj_law<1>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                              counters, st);
+                              counters, k.lists, st);
             s0 += 1;
         }
     }

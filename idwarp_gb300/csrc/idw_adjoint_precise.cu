@@ -32,8 +32,14 @@ template <int S>
 struct PrecSmem {
     static constexpr int kC = S > 0 ? 3 * S : 1;
     // leaf points reduced per shared-memory pass: a whole leaf of the default
-    // bucket (up to 9 points) in one pass for few seeds, 8 for 16 seeds
-    static constexpr int kP = S == 0 ? 1 : (S <= 4 ? 10 : 8);
+    // bucket (up to 9 points) in one pass for few seeds; 2 for 16 seeds, whose
+    // seed arrays fill shared memory (per warp 20 KB with 8 points: two blocks
+    // per SM; 16 KB with 4: three; 14 KB with 2: four; 726, 586 and 527 ms at
+    // 8M nodes)
+#ifndef IDW_PREC_KP16
+#define IDW_PREC_KP16 2
+#endif
+    static constexpr int kP = S == 0 ? 1 : (S <= 4 ? 10 : IDW_PREC_KP16);
     float nh[32][kC], nl[32][kC];      // seeds of every lane (numb, scaled), hi / lo
     float4 vh[kP][32], vl[kP][32];     // per term: w, w (r - C), hi / lo
 };
@@ -146,13 +152,14 @@ __device__ __forceinline__ void term_vector(float wh, float wl, const dfl x[3], 
 
 // S > 0: S seeds (dxv, common order, stride dxvStride) into ptAdj / nodeAdj.
 // S = 0: the denominator walk; denOut receives sum w in true units (common order).
-template <int S, int KIND>
+// REPLAY: walk the recorded decisions (idw_replay.cu) instead of deciding.
+template <int S, int KIND, int REPLAY>
 __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf, PointsDevF pf, VolumeDev v,
                                                          WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
                                                          const double *dxv, int64_t dxvStride, const double *den,
                                                          double *ptAdj, int64_t ptStride, double *nodeAdj,
                                                          int64_t nodeStride, double *denOut,
-                                                         unsigned long long *counters) {
+                                                         unsigned long long *counters, WalkLists wlists) {
     extern __shared__ __align__(16) unsigned char smraw[];
     PrecSmem<S> &sm = reinterpret_cast<PrecSmem<S> *>(smraw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -201,9 +208,22 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
         }
         __syncwarp();
         int node = 0, skip = 0;
-        while (node < t.nNodes) {
+        int64_t e = 0, e1 = 0;
+        if (REPLAY && (gid >> 5) < (v.nVol + 31) / 32) {
+            e = wlists.offs[(gid >> 5) * mp.nLoop + kk];
+            e1 = wlists.offs[(gid >> 5) * mp.nLoop + kk + 1];
+        }
+        while (REPLAY ? e < e1 : node < t.nNodes) {
+            bool active;
+            if (REPLAY) {
+                const int2 ent = __ldg(wlists.list + e);
+                ++e;
+                node = ent.x & 0x7fffffff;
+                active = (unsigned(ent.y) >> lane) & 1u;
+            } else {
+                active = valid && node >= skip;
+            }
             const int4 inf = ldgi4(&tf.nodes[node].info);
-            const bool active = valid && node >= skip;
             if (inf.w) {
                 const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                 dfl R[3];
@@ -242,16 +262,20 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                     }
                     if constexpr (S > 0) reduce_tasks_df<S>(sm, m, i0, ptAdj, ptStride);
                 }
-                node = inf.z;
+                if (!REPLAY) node = inf.z;
             } else {
                 bool open = false;
                 int dec = 0;
                 float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
-                if (active && !exact) {
-                    cnt.visited++;
-                    dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                if (REPLAY) {
+                    dec = active ? 1 : 0;
+                } else {
+                    if (active && !exact) {
+                        cnt.visited++;
+                        dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                    }
+                    dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 }
-                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 if (__any_sync(kFull, dec == 1)) {
                     float wh = 0.f, wl = 0.f;
                     dfl x[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
@@ -278,39 +302,55 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                         }
                     }
                 }
-                if (dec != 1 && active) open = true;
-                node = __any_sync(kFull, open) ? node + 1 : inf.z;
+                if (!REPLAY) {
+                    if (dec != 1 && active) open = true;
+                    node = __any_sync(kFull, open) ? node + 1 : inf.z;
+                }
             }
         }
         __syncwarp();
     }
     if (S == 0 && valid) denOut[vi] = (double(dsum) + double(dcomp)) * exp2(-double(s) * mp.bExp);
-    cnt.flush(counters);
+    if (!REPLAY) cnt.flush(counters);
 }
 
 template <int S, int KIND>
 void launch_prec(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
                  const MixedParams &mp, const Law32<KIND> &law, int exact, const double *dxv, int64_t dxvStride,
                  const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj, int64_t nodeStride,
-                 double *denOut, unsigned long long *counters, cudaStream_t st) {
+                 double *denOut, unsigned long long *counters, const WalkLists &wl, cudaStream_t st) {
     const size_t smem = 4 * sizeof(PrecSmem<S>);
-    cudaFuncSetAttribute(k_adjoint_precise<S, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     const int g = int((v.nVol + 127) / 128);
-    k_adjoint_precise<S, KIND><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den, ptAdj,
-                                                     ptStride, nodeAdj, nodeStride, denOut, counters);
+    // sixteen seeds keep deciding as they go: at four blocks per SM (shared
+    // memory) the replay's schedule measured slower (8M-node wing: 622 against
+    // 586 ms with 4 points per pass); fewer seeds replay (one seed 73 against
+    // 86 ms)
+    if (wl.list && !exact && S < 16) {
+        launch_add_walk_counters(counters, wl.counters, st);
+        cudaFuncSetAttribute(k_adjoint_precise<S, KIND, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        k_adjoint_precise<S, KIND, 1><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den,
+                                                            ptAdj, ptStride, nodeAdj, nodeStride, denOut, counters,
+                                                            wl);
+    } else {
+        cudaFuncSetAttribute(k_adjoint_precise<S, KIND, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        k_adjoint_precise<S, KIND, 0><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den,
+                                                            ptAdj, ptStride, nodeAdj, nodeStride, denOut, counters,
+                                                            wl);
+    }
 }
 
 template <int S>
 void launch_prec_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                      const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, int exact, const double *dxv,
                      int64_t dxvStride, const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj,
-                     int64_t nodeStride, double *denOut, unsigned long long *counters, cudaStream_t st) {
+                     int64_t nodeStride, double *denOut, unsigned long long *counters, const WalkLists &lists,
+                     cudaStream_t st) {
     if (wl.isInt && wl.ia == 3 && wl.ib == 5)
         launch_prec<S, 0>(t, tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, dxv, dxvStride, den, ptAdj,
-                          ptStride, nodeAdj, nodeStride, denOut, counters, st);
+                          ptStride, nodeAdj, nodeStride, denOut, counters, lists, st);
     else
         launch_prec<S, 1>(t, tf, pf, v, rec, mp, Law32<1>{wl.ia, wl.ib, float(wl.aExp), float(wl.bExp)}, exact, dxv,
-                          dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, denOut, counters, st);
+                          dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, denOut, counters, lists, st);
 }
 
 }  // namespace
@@ -323,7 +363,7 @@ void launch_precise_denominator(const TreeDev &t, const TreeDevF &tf, const Poin
     if (v.nVol <= 0) return;
     const MixedParams mp = make_mixed_params(k);
     launch_prec_law<0>(t, tf, pf, v, rec, mp, k.law, exact, nullptr, 0, nullptr, nullptr, 0, nullptr, 0, denOut,
-                       nullptr, st);
+                       nullptr, k.lists, st);
 }
 
 int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
@@ -340,15 +380,15 @@ int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDev
         double *pa = ptAcc + s0 * ptStride, *na = nodeAcc + s0 * nodeStride;
         if (left >= 16) {
             launch_prec_law<16>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                                nullptr, counters, st);
+                                nullptr, counters, k.lists, st);
             s0 += 16;
         } else if (left >= 4) {
             launch_prec_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                               nullptr, counters, st);
+                               nullptr, counters, k.lists, st);
             s0 += 4;
         } else {
             launch_prec_law<1>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                               nullptr, counters, st);
+                               nullptr, counters, k.lists, st);
             s0 += 1;
         }
     }

@@ -908,6 +908,7 @@ static int read_counters(Ctx *c) {
     c->stats.visited = int64_t(h[2]);
     c->stats.fp64Fallback = int64_t(h[3]);
     c->stats.preciseTerms = int64_t(h[6]);
+    c->stats.walkListEntries = c->listState == 1 ? c->listEntries : (c->listState == -1 ? -1 : 0);
     if (c->eventsRecorded) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->stats.lastKernelMs = ms;
@@ -1116,10 +1117,13 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
         a1.dcl = c->nodeDCl.p;
         a1.dn = c->nodeDn.p;
         a1.ref = c->refDB.p;
+        rc = ensure_walk_lists(c, tf, rec, k);
+        if (rc) return rc;
         rc = ensure_gate_den(c, tf, p1, a1, rec, k, exact);
         if (rc) return rc;
     }
     rec.gden = c->gden.p;
+    if (k.lists.list && !tiledExact && !exact) launch_add_walk_counters(c->counters.p, k.lists.counters, c->stream);
     CK(cudaEventRecord(c->ev0, c->stream));
     if (tiledExact) {
         // exact mode on a mesh that fills the GPU: the tiled kernel per surface
@@ -1405,6 +1409,8 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
+        rc = ensure_walk_lists(c, tf, rec, k);
+        if (rc) return rc;
         if (c->opt.adjointPrecision == IDW_ADJ_PRECISE && precise_adjoint_supported(k.law)) {
             // the denominator to double-float accuracy: once per weight law and mode
             if (!(c->denPValid && c->denPLdefFact == c->opt.LdefFact && c->denPAlpha == c->opt.alpha &&

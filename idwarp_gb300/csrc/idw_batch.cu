@@ -47,10 +47,13 @@ __device__ __forceinline__ void flush_partials(BatchSmem<NB> &sm, float (&pn)[NB
         }
 }
 
-template <int KIND, int NB>
+// REPLAY: walk the recorded decisions (idw_replay.cu) instead of deciding;
+// the terms, their order and their arithmetic are the deciding walk's.
+template <int KIND, int NB, int REPLAY>
 __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
     k_walk_mixed_batch(TreeDev t, TreeDevF tf, PointsDevF pf, NodeAggF af, VolumeDev v, WalkRecF rec, MixedParams mp,
-                       Law32<KIND> law, int exact, float4 *acc, int64_t accStrideB, unsigned long long *counters) {
+                       Law32<KIND> law, int exact, float4 *acc, int64_t accStrideB, unsigned long long *counters,
+                       WalkLists wlists) {
     extern __shared__ __align__(16) unsigned char smraw[];
     BatchSmem<NB> &sm = *reinterpret_cast<BatchSmem<NB> *>(smraw);
     const int tid = threadIdx.x;
@@ -93,9 +96,22 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
         float pdc = 0.f;  // cluster partial of the denominator
         int nPart = 0;    // cluster terms in the partials
         int node = 0, skip = 0;
-        while (node < t.nNodes) {
+        int64_t e = 0, e1 = 0;
+        if (REPLAY && (gid >> 5) < (v.nVol + 31) / 32) {
+            e = wlists.offs[(gid >> 5) * mp.nLoop + kk];
+            e1 = wlists.offs[(gid >> 5) * mp.nLoop + kk + 1];
+        }
+        while (REPLAY ? e < e1 : node < t.nNodes) {
+            bool active;
+            if (REPLAY) {
+                const int2 ent = __ldg(wlists.list + e);
+                ++e;
+                node = ent.x & 0x7fffffff;
+                active = (unsigned(ent.y) >> (tid & 31)) & 1u;
+            } else {
+                active = valid && node >= skip;
+            }
             const int4 inf = ldgi4(&tf.nodes[node].info);
-            const bool active = valid && node >= skip;
             if (inf.w) {
                 bool leafPrecise = false;
                 if (active) {
@@ -191,16 +207,24 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                     }
                     warp_count(counters, 6, leafPrecise ? unsigned(inf.y - inf.x + 1) : 0u);
                 }
-                node = inf.z;
+                if (!REPLAY) node = inf.z;
             } else {
                 bool open = false;
                 int dec = 0;
                 float rho0 = 0.f, rho1 = 0.f, rho2 = 0.f, d2 = 0.f, rs = 0.f, wA = 0.f;
-                if (active && !exact) {
-                    cnt.visited++;
-                    dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                if (REPLAY) {
+                    if (active) {
+                        cluster_geo(ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo), rh, rl, rho0, rho1, rho2,
+                                    d2, rs, wA);
+                        dec = 1;
+                    }
+                } else {
+                    if (active && !exact) {
+                        cnt.visited++;
+                        dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
+                    }
+                    dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 }
-                dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
                 bool precise = false;
                 if (dec == 1) {
                     const float tt = fmaf(Ls, rs, LsLo * rs);
@@ -269,7 +293,7 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
                     }
                     warp_count(counters, 6, precise ? 1u : 0u);
                 }
-                node = __any_sync(kFull, open) ? node + 1 : inf.z;
+                if (!REPLAY) node = __any_sync(kFull, open) ? node + 1 : inf.z;
             }
         }
         if (nPart) {
@@ -319,39 +343,47 @@ __global__ void __launch_bounds__(128, IDW_BATCH_MIN_BLOCKS)
             acc[b * accStrideB + 2 * gid + 1] = sm.mirC[b][tid];
         }
     }
-    cnt.flush(counters);
+    if (!REPLAY) cnt.flush(counters);
 }
 
 template <int KIND, int NB>
 void launch_batch_nb(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
                      const VolumeDev &v, const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law, int exact,
-                     float4 *acc, int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
+                     float4 *acc, int64_t accStrideB, unsigned long long *counters, const WalkLists &wl,
+                     cudaStream_t st) {
     const size_t smem = sizeof(BatchSmem<NB>);
-    cudaFuncSetAttribute(k_walk_mixed_batch<KIND, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     const int g = int((v.nVol + 127) / 128);
-    k_walk_mixed_batch<KIND, NB><<<g, 128, smem, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB,
-                                                       counters);
+    if (wl.list && !exact) {
+        cudaFuncSetAttribute(k_walk_mixed_batch<KIND, NB, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        k_walk_mixed_batch<KIND, NB, 1><<<g, 128, smem, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB,
+                                                              counters, wl);
+    } else {
+        cudaFuncSetAttribute(k_walk_mixed_batch<KIND, NB, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        k_walk_mixed_batch<KIND, NB, 0><<<g, 128, smem, st>>>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB,
+                                                              counters, wl);
+    }
 }
 
 template <int KIND>
 void launch_batch_kind(int nb, const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
                        const VolumeDev &v, const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law,
-                       int exact, float4 *acc, int64_t accStrideB, unsigned long long *counters, cudaStream_t st) {
+                       int exact, float4 *acc, int64_t accStrideB, unsigned long long *counters, const WalkLists &wl,
+                       cudaStream_t st) {
     switch (nb) {
         case 1:
-            launch_batch_nb<KIND, 1>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+            launch_batch_nb<KIND, 1>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, wl, st);
             break;
         case 2:
-            launch_batch_nb<KIND, 2>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+            launch_batch_nb<KIND, 2>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, wl, st);
             break;
         case 3:
-            launch_batch_nb<KIND, 3>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+            launch_batch_nb<KIND, 3>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, wl, st);
             break;
         case 4:
-            launch_batch_nb<KIND, 4>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+            launch_batch_nb<KIND, 4>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, wl, st);
             break;
         default:
-            launch_batch_nb<KIND, kBatchMax>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+            launch_batch_nb<KIND, kBatchMax>(t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, wl, st);
             break;
     }
 }
@@ -365,13 +397,13 @@ void launch_walk_mixed_batch(int nb, const TreeDev &t, const TreeDevF &tf, const
     const MixedParams mp = make_mixed_params(k);
     if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         Law32<0> law{3, 5, 3.f, 5.f};
-        launch_batch_kind<0>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+        launch_batch_kind<0>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, k.lists, st);
     } else if (k.law.isInt) {
         Law32<1> law{k.law.ia, k.law.ib, float(k.law.aExp), float(k.law.bExp)};
-        launch_batch_kind<1>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+        launch_batch_kind<1>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, k.lists, st);
     } else {
         Law32<2> law{0, 0, float(k.law.aExp), float(k.law.bExp)};
-        launch_batch_kind<2>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, st);
+        launch_batch_kind<2>(nb, t, tf, pf, af, v, rec, mp, law, exact, acc, accStrideB, counters, k.lists, st);
     }
 }
 

@@ -194,6 +194,8 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
 // synchronises st); launch_walk_record writes them and the walk's counters;
 // launch_walk_replay evaluates the forward sums from k.lists into acc.
 int64_t walk_list_warps(int64_t nVol);
+// dst[0..3] += the recording walk's counters (a replay counts what it replays)
+void launch_add_walk_counters(unsigned long long *dst, const unsigned long long *src, cudaStream_t st);
 int64_t count_walk_lists(const TreeDev &t, const TreeDevF &tf, const VolumeDev &v, const WalkRecF &rec,
                          const EvalConsts &k, int64_t *offs, cudaStream_t st);
 void launch_walk_record(const TreeDev &t, const TreeDevF &tf, const VolumeDev &v, const WalkRecF &rec,

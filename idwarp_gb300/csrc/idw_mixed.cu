@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
         const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
-        float sn[3] = {0, 0, 0}, cn[3] = {0, 0, 0}, sd = 0.f, cd = 0.f;
+        Sums2 rs2 = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
         int node = 0, skip = 0;
         while (node < t.nNodes) {
             const int4 inf = ldgi4(&tf.nodes[node].info);
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
             if (STATS && __any_sync(kFull, active) && counters && (threadIdx.x & 31) == 0)
                 atomicAdd(counters + (inf.w ? 4 : 5), (unsigned long long)(inf.w ? 32 * (inf.y - inf.x + 1) : 32));
             if (inf.w) {
-                leaf_step<KIND>(active, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, sn, cn, sd, cd, counters);
+                leaf_step<KIND>(active, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, rs2, counters);
                 if (active) {
                     cnt.leafPairs += inf.y - inf.x + 1;
                     cnt.visited++;
@@ -77,8 +77,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
                     dec = decide32(tf, node, rh, rl, tauf, rho0, rho1, rho2, d2, rs, wA);
                 }
                 dec = resolve64(dec, t, v, g, node, rh, rl, mp.errTol, counters);
-                approx_step<KIND>(dec == 1, tf, af, node, rho0, rho1, rho2, rs, wA, rh, rl, wl, sn, cn, sd, cd,
-                                  counters);
+                approx_step<KIND>(dec == 1, tf, af, node, rho0, rho1, rho2, rs, wA, rh, rl, wl, rs2, counters);
                 bool open = false;
                 if (dec == 1) {
                     skip = inf.z;
@@ -90,7 +89,8 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
             }
         }
         float4 S4 = mirS[threadIdx.x], C4 = mirC[threadIdx.x];
-        finish_mirror(af, mp, kk, rh, rl, sn, cn, sd, cd, S4, C4);
+        const RunSums fin = to_runsums(rs2);
+        finish_mirror(af, mp, kk, rh, rl, fin.sn, fin.cn, fin.sd, fin.cd, S4, C4);
         mirS[threadIdx.x] = S4;
         mirC[threadIdx.x] = C4;
     }
@@ -231,9 +231,7 @@ void launch_walk_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &p
     } else if (!exact && k.lists.list && !mp.slotStats) {
         // recorded decisions: the walk's terms without the walk's decisions;
         // the work counters are the recording walk's
-        if (o.counters && k.lists.counters)
-            cudaMemcpyAsync(o.counters, k.lists.counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
-                            st);
+        launch_add_walk_counters(o.counters, k.lists.counters, st);
         launch_walk_replay(tf, pf, af, v, rec, k, acc, o.counters, st);
     } else if (k.law.isInt && k.law.ia == 3 && k.law.ib == 5) {
         launch_walk_kind(g, t, tf, pf, af, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, acc, o.counters, st);

@@ -65,6 +65,34 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
     s = t;
 }
 
+// Packed FP32 pairs (the f32x2 instructions of sm_100 and later): each half
+// is rounded exactly as the scalar operation, so a packed sequence gives the
+// scalar results bit for bit with one instruction issued for two.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<const unsigned long long *>(&a)), "l"(*reinterpret_cast<const unsigned long long *>(&b)));
+    return *reinterpret_cast<const float2 *>(&d);
+}
+
+// kahan_add on two independent pairs at once (bitwise two kahan_add calls).
+__device__ __forceinline__ void kahan_add2(float2 &s, float2 &c, float2 x) {
+    const float2 t = add2(s, x);
+    const float2 bp = sub2(t, s);
+    c = add2(c, add2(sub2(s, sub2(t, bp)), sub2(x, bp)));
+    s = t;
+}
+
+// Running sums of one mirror pass in the forward walks: numerator and
+// denominator, each a compensated pair (sum = s + c), packed as (num0, num1)
+// and (num2, den) for kahan_add2.
+struct Sums2 {
+    float2 s01, s2d, c01, c2d;
+};
+
 __device__ __forceinline__ float4 ldgf4(const float4 *p) { return __ldg(p); }
 __device__ __forceinline__ int4 ldgi4(const int4 *p) { return __ldg(p); }
 
@@ -463,6 +491,19 @@ __device__ __forceinline__ bool leaf_close(float pn0, float pn1, float pn2, floa
     return precise;
 }
 
+// leaf_close on the packed running sums (the same gate, bitwise the same sums).
+template <int KIND>
+__device__ __forceinline__ bool leaf_close2(float pn0, float pn1, float pn2, float pd, float dn, float h0, float h1,
+                                            float h2, float gv, Sums2 &r) {
+    const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + pd * dn * (fabsf(h0) + fabsf(h1) + fabsf(h2));
+    const bool precise = KIND != 2 && lmag > gv;
+    if (!precise) {
+        kahan_add2(r.s01, r.c01, make_float2(pn0, pn1));
+        kahan_add2(r.s2d, r.c2d, make_float2(pn2, pd));
+    }
+    return precise;
+}
+
 // A leaf's terms (points lo..hi) re-summed in double-float.
 template <int KIND>
 __device__ __forceinline__ void precise_leaf(const TreeDevF &tf, const PointsDevF &pf, int node, int lo, int hi,
@@ -497,6 +538,13 @@ __device__ __forceinline__ void precise_leaf(const TreeDevF &tf, const PointsDev
 struct RunSums {
     float sn[3], cn[3], sd, cd;
 };
+__device__ __forceinline__ RunSums to_runsums(const Sums2 &r) {
+    return {{r.s01.x, r.s01.y, r.s2d.x}, {r.c01.x, r.c01.y, r.c2d.x}, r.s2d.y, r.c2d.y};
+}
+__device__ __forceinline__ Sums2 from_runsums(const RunSums &a) {
+    return {make_float2(a.sn[0], a.sn[1]), make_float2(a.sn[2], a.sd), make_float2(a.cn[0], a.cn[1]),
+            make_float2(a.cn[2], a.cd)};
+}
 
 // A cluster term in double-float (the walk's precision gate sent it here):
 // h + l is the split volume point, ch/cl the split centroid (cl.w = area hi),
@@ -546,8 +594,7 @@ struct WalkLane {
 template <int KIND>
 __device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
                                           int node, int lo, int hi, const float *rh, const float *rl,
-                                          const WalkLane<KIND> &wl, float *sn, float *cn, float &sd, float &cd,
-                                          unsigned long long *counters) {
+                                          const WalkLane<KIND> &wl, Sums2 &r, unsigned long long *counters) {
     bool leafPrecise = false;
     if (mine) {
         const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
@@ -568,17 +615,12 @@ __device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const P
         }
         // a leaf carrying a large weight at a long lever arm is re-summed in
         // double-float (same gate as cluster terms)
-        leafPrecise = leaf_close<KIND>(pn0, pn1, pn2, pd, __ldg(af.dn + node), h0, h1, h2, wl.gv, sn, cn, sd, cd);
+        leafPrecise = leaf_close2<KIND>(pn0, pn1, pn2, pd, __ldg(af.dn + node), h0, h1, h2, wl.gv, r);
     }
     if (__any_sync(kFull, leafPrecise)) {
-        if (leafPrecise) {
-            RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
-            a = precise_leaf_ool<KIND>(a, tf, pf, node, lo, hi, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2], wl.law,
-                                       wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl);
-            sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
-            cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
-            sd = a.sd, cd = a.cd;
-        }
+        if (leafPrecise)
+            r = from_runsums(precise_leaf_ool<KIND>(to_runsums(r), tf, pf, node, lo, hi, rh[0], rh[1], rh[2], rl[0],
+                                                    rl[1], rl[2], wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl));
         warp_count(counters, 6, leafPrecise ? unsigned(hi - lo + 1) : 0u);
     }
 }
@@ -589,8 +631,8 @@ __device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const P
 template <int KIND>
 __device__ __forceinline__ void approx_step(bool mine, const TreeDevF &tf, const NodeAggF &af, int node, float rho0,
                                             float rho1, float rho2, float rs, float wA, const float *rh,
-                                            const float *rl, const WalkLane<KIND> &wl, float *sn, float *cn,
-                                            float &sd, float &cd, unsigned long long *counters) {
+                                            const float *rl, const WalkLane<KIND> &wl, Sums2 &r,
+                                            unsigned long long *counters) {
     bool precise = false;
     if (mine) {
         const float tt = fmaf(wl.Ls, rs, wl.LsLo * rs);
@@ -606,22 +648,17 @@ __device__ __forceinline__ void approx_step(bool mine, const TreeDevF &tf, const
                           __ldg(af.dn + node) * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
         precise = KIND != 2 && w * mag > wl.gv;
         if (!precise) {
-            kahan_add(sn[0], cn[0], w * S0);
-            kahan_add(sn[1], cn[1], w * S1);
-            kahan_add(sn[2], cn[2], w * S2);
-            kahan_add(sd, cd, w);
+            const float2 ww = make_float2(w, w);
+            kahan_add2(r.s01, r.c01, mul2(make_float2(S0, S1), ww));
+            kahan_add2(r.s2d, r.c2d, mul2(make_float2(S2, 1.0f), ww));
         }
     }
     if (__any_sync(kFull, precise)) {
-        if (precise) {
-            RunSums a = {{sn[0], sn[1], sn[2]}, {cn[0], cn[1], cn[2]}, sd, cd};
-            a = precise_cluster<KIND>(a, rh[0], rh[1], rh[2], rl[0], rl[1], rl[2], ldgf4(&tf.nodes[node].cHi),
-                                      ldgf4(&tf.nodes[node].cLo), __ldg(&tf.nodes[node].aLo), af.dc + 12 * node,
-                                      af.dcl + 12 * node, wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl);
-            sn[0] = a.sn[0], sn[1] = a.sn[1], sn[2] = a.sn[2];
-            cn[0] = a.cn[0], cn[1] = a.cn[1], cn[2] = a.cn[2];
-            sd = a.sd, cd = a.cd;
-        }
+        if (precise)
+            r = from_runsums(precise_cluster<KIND>(to_runsums(r), rh[0], rh[1], rh[2], rl[0], rl[1], rl[2],
+                                                   ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo),
+                                                   __ldg(&tf.nodes[node].aLo), af.dc + 12 * node, af.dcl + 12 * node,
+                                                   wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl));
         warp_count(counters, 6, precise ? 1u : 0u);
     }
 }

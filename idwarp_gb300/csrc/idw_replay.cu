@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS)
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
         const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
-        float sn[3] = {0, 0, 0}, cn[3] = {0, 0, 0}, sd = 0.f, cd = 0.f;
+        Sums2 rs2 = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
         const int64_t e1 = offs[warp * mp.nLoop + kk + 1];
         for (int64_t e = offs[warp * mp.nLoop + kk]; e < e1; ++e) {
             const int2 ent = __ldg(list + e);
@@ -129,17 +129,17 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS)
             const bool mine = (unsigned(ent.y) >> lane) & 1u;
             if (ent.x < 0) {
                 const int4 inf = ldgi4(&tf.nodes[node].info);
-                leaf_step<KIND>(mine, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, sn, cn, sd, cd, counters);
+                leaf_step<KIND>(mine, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, rs2, counters);
             } else {
                 const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                 float rho0, rho1, rho2, d2, rs, wA;
                 cluster_geo(ch, cl, rh, rl, rho0, rho1, rho2, d2, rs, wA);
-                approx_step<KIND>(mine, tf, af, node, rho0, rho1, rho2, rs, wA, rh, rl, wl, sn, cn, sd, cd,
-                                  counters);
+                approx_step<KIND>(mine, tf, af, node, rho0, rho1, rho2, rs, wA, rh, rl, wl, rs2, counters);
             }
         }
         float4 S4 = mirS[threadIdx.x], C4 = mirC[threadIdx.x];
-        finish_mirror(af, mp, kk, rh, rl, sn, cn, sd, cd, S4, C4);
+        const RunSums fin = to_runsums(rs2);
+        finish_mirror(af, mp, kk, rh, rl, fin.sn, fin.cn, fin.sd, fin.cd, S4, C4);
         mirS[threadIdx.x] = S4;
         mirC[threadIdx.x] = C4;
     }
@@ -147,6 +147,10 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS)
         acc[2 * gid] = mirS[threadIdx.x];
         acc[2 * gid + 1] = mirC[threadIdx.x];
     }
+}
+
+__global__ void k_add_counters(int n, const unsigned long long *src, unsigned long long *dst) {
+    if (int(threadIdx.x) < n) dst[threadIdx.x] += src[threadIdx.x];
 }
 
 inline int blocks(int64_t n, int b) { return int((n + b - 1) / b); }
@@ -163,6 +167,10 @@ void replay_kind(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, c
 }  // namespace
 
 int64_t walk_list_warps(int64_t nVol) { return (nVol + 31) / 32; }
+
+void launch_add_walk_counters(unsigned long long *dst, const unsigned long long *src, cudaStream_t st) {
+    if (dst && src) k_add_counters<<<1, 32, 0, st>>>(4, src, dst);
+}
 
 int64_t count_walk_lists(const TreeDev &t, const TreeDevF &tf, const VolumeDev &v, const WalkRecF &rec,
                          const EvalConsts &k, int64_t *offs, cudaStream_t st) {

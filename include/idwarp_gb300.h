@@ -113,7 +113,7 @@ typedef struct idw_stats {
     int64_t warpLeafSlots; /* lane slots of warp-level leaf visits (32 x leaf size); leafPairs / this = lane use */
     int64_t warpNodeSlots; /* lane slots of warp-level interior-node visits (32 per visit) */
     int64_t preciseTerms;  /* mixed mode: cluster terms summed in double-float */
-    int64_t reserved[1];
+    int64_t walkListEntries; /* recorded walk decisions (8 bytes each; -1: too large, walks decide) */
 } idw_stats;
 
 /* Fill `o` with the reference defaults (idwarp/UnstructuredMesh.py:124-145). */

@@ -109,3 +109,58 @@ def test_few_volume_nodes(built_lib):
     np.testing.assert_array_equal(a[0], b[0])
     for k in STATS:
         assert a[1][k] == b[1][k], k
+
+
+def test_batched_surfaces_replay(built_lib):
+    # five surfaces: a group of four and one alone, each replayed
+    m = _mesh("wing", 0)
+    rng = np.random.default_rng(5)
+    surfs = np.stack([m["xs"] + 1e-3 * rng.standard_normal(m["xs"].shape) for _ in range(5)])
+    res = []
+    for wl in ("auto", "off"):
+        g = build_gpu(m, {"walkLists": wl}, precision="mixed")
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        res.append((g.warpMeshBatch(surfs), g.getStats()))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    for k in ("leafPairs", "approx", "visited"):
+        assert res[0][1][k] == res[1][1][k], k
+
+
+def test_batched_tangents_replay(built_lib):
+    m = _mesh("sphere", 1)
+    rng = np.random.default_rng(6)
+    dirs = rng.standard_normal((3,) + m["xs"].shape)
+    res = []
+    for wl in ("auto", "off"):
+        g = build_gpu(m, {"walkLists": wl}, precision="mixed")
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        res.append(g.warpDerivFwdBatch(dirs))
+    np.testing.assert_array_equal(res[0], res[1])
+
+
+@pytest.mark.parametrize("prec", ["precise", "fast"])
+@pytest.mark.parametrize("nseeds", [1, 21])
+def test_reverse_product_replay(prec, nseeds, built_lib):
+    # the adjoint lands warp sums with FP64 atomics, whose order varies from
+    # run to run: the replayed and the deciding walk agree to that rounding
+    m = _mesh("wing", 0)
+    rng = np.random.default_rng(9)
+    nvol = len(m["xv0"])
+    dxv = rng.standard_normal((nseeds, nvol, 3))
+    res = []
+    for wl in ("auto", "off"):
+        g = build_gpu(m, {"walkLists": wl, "adjointPrecision": prec}, precision="mixed")
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        if nseeds == 1:
+            g.warpDeriv(dxv[0].ravel(), solverVec=False)
+            out = g.getdXs()[None]
+        else:
+            out = g.warpDerivBatch(dxv)
+        res.append((out, g.getStats()))
+    scale = np.abs(res[1][0]).max()
+    assert np.abs(res[0][0] - res[1][0]).max() <= 1e-11 * scale
+    for k in ("leafPairs", "approx", "visited", "fp64Fallback"):
+        assert res[0][1][k] == res[1][1][k], k
