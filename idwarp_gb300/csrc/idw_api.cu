@@ -312,7 +312,7 @@ int finish_den0(Ctx *c) {
 int ensure_den0(Ctx *c) {
     if (c->den0Valid) return IDW_OK;
     CK(cudaSetDevice(c->device));
-    launch_denominator0(tree_dev(c), c->ptXA.p, vol_dev(c), make_init_law(c), c->sym, c->den0.p, c->stream);
+    launch_denominator0(tree_dev(c), c->nodeRec.p, c->ptXA.p, vol_dev(c), make_init_law(c), c->sym, c->den0.p, c->stream);
     int e = check_launch(c, "denominator0");
     if (e) return e;
     return finish_den0(c);
@@ -1318,7 +1318,7 @@ int idw_set_denominator0(void *ctx, const double *den0, int64_t nvol, int64_t ch
         const int64_t m = (nvol + checkStride - 1) / checkStride;
         DevBuf<double> est;
         CKA(est.alloc(size_t(m)));
-        launch_denominator0_strided(tree_dev(c), c->ptXA.p, vol_dev(c), make_init_law(c), c->sym, checkStride,
+        launch_denominator0_strided(tree_dev(c), c->nodeRec.p, c->ptXA.p, vol_dev(c), make_init_law(c), c->sym, checkStride,
                                     est.p, st);
         rc = check_launch(c, "denominator0 check");
         if (rc) return rc;

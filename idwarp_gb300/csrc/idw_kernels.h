@@ -161,11 +161,13 @@ void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, co
 // Set-up kernels (idw_setup.cu)
 // Returns 0, -1 on a CUDA error, -2 when its scratch cannot be allocated.
 int launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &law, double *err, cudaStream_t st);
-void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
-                         const SymPlanes &sym, double *den0, cudaStream_t st);
+// rf: the FP32 node records (split centroid, radius) for the guarded FP32 far-field test
+void launch_denominator0(const TreeDev &t, const NodeRecF *rf, const dbl4 *ptXA, const VolumeDev &v,
+                         const WeightLaw &law, const SymPlanes &sym, double *den0, cudaStream_t st);
 // estimate of the common-order nodes 0, stride, 2 stride, ... into out; returns their count
-int64_t launch_denominator0_strided(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
-                                    const SymPlanes &sym, int64_t stride, double *out, cudaStream_t st);
+int64_t launch_denominator0_strided(const TreeDev &t, const NodeRecF *rf, const dbl4 *ptXA, const VolumeDev &v,
+                                    const WeightLaw &law, const SymPlanes &sym, int64_t stride, double *out,
+                                    cudaStream_t st);
 void launch_dry_run(const TreeDev &t, const VolumeDev &v, const SymPlanes &sym, double errTol, int nPts,
                     double *costs, cudaStream_t st);
 // Bounding box of n points on the device and the number of non-finite

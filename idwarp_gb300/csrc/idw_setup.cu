@@ -121,8 +121,17 @@ __global__ void k_err_final(TreeDev t, WeightLaw law, const int *nodeItem0, cons
 // rule; every lane follows exactly its own recursion of getWiEstimate.
 // stride 0: every node in Morton order, out[common index]; stride > 0: the
 // common-order nodes 0, stride, 2 stride, ... (nOut of them), out[k].
-__global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, SymPlanes sym, int64_t stride,
-                       int64_t nOut, double *out) {
+//
+// The far-field test dist * oradius > 5 is first taken in FP32 from the split
+// centroid of the node records (rf): the volume point split in two floats, r
+// - C formed from the splits, |r - C|^2 + 1e-16 and its square root; it
+// stands when it is further than 4e-6 (relative) from 5, which bounds its
+// FP32 rounding (a few 1e-7) once |r - C|^2 >= 1e-12 (the splits' own
+// representation error, ~1e-13 absolute, is then below 1e-7 relative).
+// Otherwise, and for every approximated cluster's term, the test and the
+// distance are FP64, so decisions and terms are the FP64 walk's.
+__global__ void k_den0(TreeDev t, const NodeRecF *rf, const dbl4 *ptXA, VolumeDev v, WeightLaw law, SymPlanes sym,
+                       int64_t stride, int64_t nOut, double *out) {
     const int64_t gid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const bool valid = gid < nOut;
     const int vi = !valid ? 0 : (stride > 0 ? int(gid * stride) : v.perm[gid]);
@@ -131,6 +140,12 @@ __global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, 
     for (int kk = 0; kk < sym.nLoop; ++kk) {
         double r[3];
         mirror_point(sym, kk, x0, r);
+        float rh[3], rl[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            rh[c] = float(r[c]);
+            rl[c] = float(r[c] - double(rh[c]));
+        }
         int node = 0, skip = 0;
         while (node < t.nNodes) {
             const int4 inf = t.info[node];
@@ -148,12 +163,26 @@ __global__ void k_den0(TreeDev t, const dbl4 *ptXA, VolumeDev v, WeightLaw law, 
             } else {
                 bool open = false;
                 if (active) {
-                    const dbl4 g = t.geom[node];
-                    double r0 = r[0] - g.x, r1 = r[1] - g.y, r2 = r[2] - g.z;
-                    double dist = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + 1e-16);
-                    if (dist * g.w > 5.0) {
-                        acc += t.ai[node] * law64(law, law.Ldef / dist);
-                        skip = inf.z;
+                    // 0 open, 1 far field, 2 undecided in FP32
+                    int dec = 2;
+                    const float4 ch = __ldg(&rf[node].cHi), cl = __ldg(&rf[node].cLo);
+                    const float f0 = (rh[0] - ch.x) + (rl[0] - cl.x), f1 = (rh[1] - ch.y) + (rl[1] - cl.y),
+                                f2 = (rh[2] - ch.z) + (rl[2] - cl.z);
+                    const float d2f = fmaf(f0, f0, fmaf(f1, f1, fmaf(f2, f2, 1e-16f)));
+                    if (d2f >= 1e-12f) {
+                        const float xf = sqrtf(d2f) * ch.w;
+                        dec = xf > 5.0f * (1.0f + 4e-6f) ? 1 : (xf < 5.0f * (1.0f - 4e-6f) ? 0 : 2);
+                    }
+                    if (dec != 0) {
+                        const dbl4 g = t.geom[node];
+                        double r0 = r[0] - g.x, r1 = r[1] - g.y, r2 = r[2] - g.z;
+                        double dist = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + 1e-16);
+                        if (dec == 1 || dist * g.w > 5.0) {
+                            acc += t.ai[node] * law64(law, law.Ldef / dist);
+                            skip = inf.z;
+                        } else {
+                            open = true;
+                        }
                     } else {
                         open = true;
                     }
@@ -425,15 +454,16 @@ int launch_compute_errors(const TreeDev &t, const dbl4 *ptXA, const WeightLaw &l
     return rc;
 }
 
-void launch_denominator0(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
-                         const SymPlanes &sym, double *den0, cudaStream_t st) {
-    if (v.nVol > 0) k_den0<<<blocks(v.nVol, 128), 128, 0, st>>>(t, ptXA, v, law, sym, 0, v.nVol, den0);
+void launch_denominator0(const TreeDev &t, const NodeRecF *rf, const dbl4 *ptXA, const VolumeDev &v,
+                         const WeightLaw &law, const SymPlanes &sym, double *den0, cudaStream_t st) {
+    if (v.nVol > 0) k_den0<<<blocks(v.nVol, 128), 128, 0, st>>>(t, rf, ptXA, v, law, sym, 0, v.nVol, den0);
 }
 
-int64_t launch_denominator0_strided(const TreeDev &t, const dbl4 *ptXA, const VolumeDev &v, const WeightLaw &law,
-                                    const SymPlanes &sym, int64_t stride, double *out, cudaStream_t st) {
+int64_t launch_denominator0_strided(const TreeDev &t, const NodeRecF *rf, const dbl4 *ptXA, const VolumeDev &v,
+                                    const WeightLaw &law, const SymPlanes &sym, int64_t stride, double *out,
+                                    cudaStream_t st) {
     const int64_t n = stride > 0 ? (v.nVol + stride - 1) / stride : 0;
-    if (n > 0) k_den0<<<blocks(n, 128), 128, 0, st>>>(t, ptXA, v, law, sym, stride, n, out);
+    if (n > 0) k_den0<<<blocks(n, 128), 128, 0, st>>>(t, rf, ptXA, v, law, sym, stride, n, out);
     return n;
 }
 
