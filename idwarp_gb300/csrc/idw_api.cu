@@ -99,6 +99,7 @@ struct Ctx {
     double denPLdefFact = 0.0, denPAlpha = 0.0;
     int denPMode = -1;
     DevBuf<float> ptDM, ptDMl, nodeDC, nodeDCl, nodeDn, refDB;
+    DevBuf<float4> replayRec;  // NodeAggF::rr: 8 float4 per tree node
     // recorded decisions of the fast walk (idw_replay.cu), valid for the
     // current den0 and listErrTol; listState 1 = recorded, -1 = too large
     // (the walks decide as they go), 0 = not yet recorded
@@ -290,6 +291,7 @@ int refresh_nodal(Ctx *c) {
                            c->stream);
         launch_mixed_nodes(tree_dev(c), c->nodeMB.p, c->ptMB.p, c->nodeDC.p, c->nodeDCl.p, c->nodeDn.p, c->refDB.p,
                            c->stream);
+        launch_replay_records(c->nNodes, c->nodeDC.p, c->nodeDn.p, c->replayRec.p, c->stream);
     }
     c->nodalValid = true;
     return check_launch(c, "nodal properties");
@@ -698,6 +700,27 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
             }
         }
         CK(cudaMemcpyAsync(c->nodeRec.p, recs.data(), sizeof(NodeRecF) * nn, cudaMemcpyHostToDevice, st));
+        // static fields of the replay records; dn and dc follow per surface
+        {
+            std::vector<float4> rr(8 * size_t(nn), make_float4(0.f, 0.f, 0.f, 0.f));
+            const auto bits = [](int v) {
+                float f;
+                std::memcpy(&f, &v, sizeof(f));
+                return f;
+            };
+            for (int k = 0; k < nn; ++k) {
+                float4 *r = rr.data() + 8 * size_t(k);
+                r[0] = make_float4(recs[k].cHi.x, recs[k].cHi.y, recs[k].cHi.z, 0.f);
+                r[1] = recs[k].cLo;
+                if (t.leaf[k]) {
+                    r[1].w = bits(t.l[k]);
+                    r[2].x = bits(t.u[k]);
+                    r[5].x = bits(1);
+                }
+            }
+            CKA(c->replayRec.alloc(rr.size()));
+            CK(cudaMemcpyAsync(c->replayRec.p, rr.data(), sizeof(float4) * rr.size(), cudaMemcpyHostToDevice, st));
+        }
         CK(cudaMemcpyAsync(c->ptDA.p, da.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(c->ptDL.p, dl.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, st));
         CK(cudaStreamSynchronize(st));
@@ -879,6 +902,7 @@ static int run_warp(Ctx *c, double *xvOut, double *denOut) {
         af.dcl = c->nodeDCl.p;
         af.dn = c->nodeDn.p;
         af.ref = c->refDB.p;
+        af.rr = c->replayRec.p;
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;
@@ -1117,6 +1141,7 @@ static int run_warp_batch_mixed(Ctx *c, const double *coordsDev, int nb, double 
         a1.dcl = c->nodeDCl.p;
         a1.dn = c->nodeDn.p;
         a1.ref = c->refDB.p;
+        a1.rr = c->replayRec.p;
         rc = ensure_walk_lists(c, tf, rec, k);
         if (rc) return rc;
         rc = ensure_gate_den(c, tf, p1, a1, rec, k, exact);
@@ -1607,6 +1632,7 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
         launch_mixed_nodal(n, tree_dev(c), nodeMBd.p, c->ptXA.p, ptMBd.p, c->ptDM.p, c->ptDMl.p, c->stream);
         launch_mixed_nodes(tree_dev(c), nodeMBd.p, ptMBd.p, c->nodeDC.p, c->nodeDCl.p, c->nodeDn.p, c->refDB.p,
                            c->stream);
+        launch_replay_records(c->nNodes, c->nodeDC.p, c->nodeDn.p, c->replayRec.p, c->stream);
         c->nodalValid = false;
         const TreeDevF tf = tree_devf(c);
         PointsDevF pf;
@@ -1619,6 +1645,7 @@ int run_deriv_fwd(Ctx *c, const double *xsdDev, double *xvdDev) {
         af.dcl = c->nodeDCl.p;
         af.dn = c->nodeDn.p;
         af.ref = c->refDB.p;
+        af.rr = c->replayRec.p;
         WalkRecF rec;
         rec.hi = c->recHi.p;
         rec.lo = c->recLo.p;

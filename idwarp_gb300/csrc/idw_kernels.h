@@ -92,6 +92,11 @@ struct NodeAggF {
     const float *dcl;    // the same, low parts
     const float *dn;     // per node: bound on |D'| (max absolute row sum)
     const float *ref;    // reference motion Dref (9), bref (3): high parts, then low parts
+    // per node, what a replayed step reads, in one 128-byte record (8 float4):
+    // (cHi.xyz, dn), (cLo.xyz, area; a leaf: first point as int bits),
+    // dc high parts (12 floats; a leaf: last point as int bits in .x),
+    // (leaf flag as int bits, 0, 0, 0), pad
+    const float4 *rr = nullptr;
 };
 
 struct VolumeDev {
@@ -180,6 +185,8 @@ void launch_morton_codes(int64_t nVol, const double *xv0, const double *lo, cons
 // point-major arrays); dnStride likewise for nodeDn.
 void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl4 *ptXA, const double *ptMB,
                         float *ptDM, float *ptDMl, cudaStream_t st, int pStride = 12);
+// The per-surface fields of the replay records (dn, dc) from nodeDn / nodeDC.
+void launch_replay_records(int nNodes, const float *nodeDC, const float *nodeDn, float4 *rr, cudaStream_t st);
 void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
                         float *nodeDn, float *refDB, cudaStream_t st, int nStride = 12, int dnStride = 1);
 

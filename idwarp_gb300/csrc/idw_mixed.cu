@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS) k_walk_mixed(TreeDev
             if (STATS && __any_sync(kFull, active) && counters && (threadIdx.x & 31) == 0)
                 atomicAdd(counters + (inf.w ? 4 : 5), (unsigned long long)(inf.w ? 32 * (inf.y - inf.x + 1) : 32));
             if (inf.w) {
-                leaf_step<KIND>(active, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, rs2, counters);
+                leaf_step<KIND>(active, tf, pf, node, inf.x, inf.y, &tf.nodes[node].cHi, &tf.nodes[node].cLo,
+                                af.dn + node, rh, rl, wl, rs2, counters);
                 if (active) {
                     cnt.leafPairs += inf.y - inf.x + 1;
                     cnt.visited++;

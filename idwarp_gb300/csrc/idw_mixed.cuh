@@ -589,15 +589,18 @@ struct WalkLane {
 };
 
 // A leaf summed by the lanes with `mine` set: pair terms relative to the leaf
-// centroid, partial sums into the running pairs, and heavy leaves (the gate of
-// leaf_close) re-summed in double-float.  Called by all 32 lanes.
+// centroid (split in *chp + *clp; .w unused), partial sums into the running
+// pairs, and heavy leaves (the gate of leaf_close with the leaf's |D'| bound
+// *dnp) re-summed in double-float.  Called by all 32 lanes; the record
+// pointers let the deciding walk and the replay read their own layouts.
 template <int KIND>
-__device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af,
-                                          int node, int lo, int hi, const float *rh, const float *rl,
-                                          const WalkLane<KIND> &wl, Sums2 &r, unsigned long long *counters) {
+__device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const PointsDevF &pf, int node, int lo,
+                                          int hi, const float4 *chp, const float4 *clp, const float *dnp,
+                                          const float *rh, const float *rl, const WalkLane<KIND> &wl, Sums2 &r,
+                                          unsigned long long *counters) {
     bool leafPrecise = false;
     if (mine) {
-        const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+        const float4 ch = ldgf4(chp), cl = ldgf4(clp);
         // r - C as hi + lo: exact high parts, so a volume node on a surface
         // node resolves d^2 = eps (1e-15) to full precision
         float h0, h1, h2, l0, l1, l2;
@@ -615,7 +618,7 @@ __device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const P
         }
         // a leaf carrying a large weight at a long lever arm is re-summed in
         // double-float (same gate as cluster terms)
-        leafPrecise = leaf_close2<KIND>(pn0, pn1, pn2, pd, __ldg(af.dn + node), h0, h1, h2, wl.gv, r);
+        leafPrecise = leaf_close2<KIND>(pn0, pn1, pn2, pd, __ldg(dnp), h0, h1, h2, wl.gv, r);
     }
     if (__any_sync(kFull, leafPrecise)) {
         if (leafPrecise)
@@ -625,9 +628,50 @@ __device__ __forceinline__ void leaf_step(bool mine, const TreeDevF &tf, const P
     }
 }
 
-// A cluster approximated by the lanes with `mine` set, from its geometry
-// (cluster_geo): w = A law(L/d), S = D' (r - C) + c'; terms with a large weight
-// at a long lever arm are re-evaluated in double-float.  Called by all 32 lanes.
+// One cluster term from its geometry (cluster_geo) and the cluster's D', c'
+// (m0..m2, 12 floats) and |D'| bound dn: w = A law(L/d), S = D' (r - C) + c',
+// added to the running pairs unless the term carries a large weight at a long
+// lever arm (then returns true: the caller re-evaluates it in double-float).
+template <int KIND>
+__device__ __forceinline__ bool approx_add(const float4 m0, const float4 m1, const float4 m2, float dn, float rho0,
+                                           float rho1, float rho2, float rs, float wA, const WalkLane<KIND> &wl,
+                                           Sums2 &r) {
+    const float tt = fmaf(wl.Ls, rs, wl.LsLo * rs);
+    const float w = wA * wl.law.eval(tt, wl.c1, wl.ab, wl.abl);
+    const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
+    const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
+    const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
+    const float mag = fabsf(S0) + fabsf(S1) + fabsf(S2) + dn * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
+    const bool precise = KIND != 2 && w * mag > wl.gv;
+    if (!precise) {
+        const float2 ww = make_float2(w, w);
+        kahan_add2(r.s01, r.c01, mul2(make_float2(S0, S1), ww));
+        kahan_add2(r.s2d, r.c2d, mul2(make_float2(S2, 1.0f), ww));
+    }
+    return precise;
+}
+
+// The double-float re-evaluation of the cluster terms approx_add declined.
+// Called by all 32 lanes.
+template <int KIND>
+__device__ __forceinline__ void approx_vote(bool precise, const TreeDevF &tf, const NodeAggF &af, int node,
+                                            const float *rh, const float *rl, const WalkLane<KIND> &wl, Sums2 &r,
+                                            unsigned long long *counters) {
+    if (__any_sync(kFull, precise)) {
+        if (precise)
+            r = from_runsums(precise_cluster<KIND>(to_runsums(r), rh[0], rh[1], rh[2], rl[0], rl[1], rl[2],
+                                                   ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo),
+                                                   __ldg(&tf.nodes[node].aLo), af.dc + 12 * node, af.dcl + 12 * node,
+                                                   wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl));
+        warp_count(counters, 6, precise ? 1u : 0u);
+    }
+}
+
+// A cluster approximated by the lanes with `mine` set (the deciding walk:
+// the cluster's motion is loaded where a lane approximates).  The arithmetic
+// is approx_add's, written out here: inlined through approx_add the deciding
+// walk's register allocation spilled five times more.  Called by all 32
+// lanes.
 template <int KIND>
 __device__ __forceinline__ void approx_step(bool mine, const TreeDevF &tf, const NodeAggF &af, int node, float rho0,
                                             float rho1, float rho2, float rs, float wA, const float *rh,
@@ -642,8 +686,6 @@ __device__ __forceinline__ void approx_step(bool mine, const TreeDevF &tf, const
         const float S0 = fmaf(m0.x, rho0, fmaf(m0.y, rho1, fmaf(m0.z, rho2, m2.y)));
         const float S1 = fmaf(m0.w, rho0, fmaf(m1.x, rho1, fmaf(m1.y, rho2, m2.z)));
         const float S2 = fmaf(m1.z, rho0, fmaf(m1.w, rho1, fmaf(m2.x, rho2, m2.w)));
-        // a far cluster with a large weight at a long lever arm is
-        // re-evaluated in double-float below
         const float mag = fabsf(S0) + fabsf(S1) + fabsf(S2) +
                           __ldg(af.dn + node) * (fabsf(rho0) + fabsf(rho1) + fabsf(rho2));
         precise = KIND != 2 && w * mag > wl.gv;
@@ -653,14 +695,7 @@ __device__ __forceinline__ void approx_step(bool mine, const TreeDevF &tf, const
             kahan_add2(r.s2d, r.c2d, mul2(make_float2(S2, 1.0f), ww));
         }
     }
-    if (__any_sync(kFull, precise)) {
-        if (precise)
-            r = from_runsums(precise_cluster<KIND>(to_runsums(r), rh[0], rh[1], rh[2], rl[0], rl[1], rl[2],
-                                                   ldgf4(&tf.nodes[node].cHi), ldgf4(&tf.nodes[node].cLo),
-                                                   __ldg(&tf.nodes[node].aLo), af.dc + 12 * node, af.dcl + 12 * node,
-                                                   wl.law, wl.Ls, wl.LsLo, wl.c1, wl.ab, wl.abl));
-        warp_count(counters, 6, precise ? 1u : 0u);
-    }
+    approx_vote<KIND>(precise, tf, af, node, rh, rl, wl, r, counters);
 }
 
 // End of one mirror pass: add the reference motion back, num += den (Dref r +

@@ -127,14 +127,19 @@ __global__ void __launch_bounds__(128, IDW_WALK_MIN_BLOCKS)
             const int2 ent = __ldg(list + e);
             const int node = ent.x & ~kLeafBit;
             const bool mine = (unsigned(ent.y) >> lane) & 1u;
+            // the node's replay record: one 128-byte line
+            const float4 *rr = af.rr + 8 * int64_t(node);
             if (ent.x < 0) {
-                const int4 inf = ldgi4(&tf.nodes[node].info);
-                leaf_step<KIND>(mine, tf, pf, af, node, inf.x, inf.y, rh, rl, wl, rs2, counters);
+                leaf_step<KIND>(mine, tf, pf, node, __float_as_int(__ldg(&rr[1].w)), __float_as_int(__ldg(&rr[2].x)),
+                                rr, rr + 1, &rr[0].w, rh, rl, wl, rs2, counters);
             } else {
-                const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
+                const float4 c0 = ldgf4(rr), c1 = ldgf4(rr + 1);
                 float rho0, rho1, rho2, d2, rs, wA;
-                cluster_geo(ch, cl, rh, rl, rho0, rho1, rho2, d2, rs, wA);
-                approx_step<KIND>(mine, tf, af, node, rho0, rho1, rho2, rs, wA, rh, rl, wl, rs2, counters);
+                cluster_geo(c0, c1, rh, rl, rho0, rho1, rho2, d2, rs, wA);
+                bool precise = false;
+                if (mine) precise = approx_add<KIND>(ldgf4(rr + 2), ldgf4(rr + 3), ldgf4(rr + 4), c0.w, rho0, rho1,
+                                                     rho2, rs, wA, wl, rs2);
+                approx_vote<KIND>(precise, tf, af, node, rh, rl, wl, rs2, counters);
             }
         }
         float4 S4 = mirS[threadIdx.x], C4 = mirC[threadIdx.x];

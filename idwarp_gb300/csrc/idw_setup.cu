@@ -513,6 +513,23 @@ void launch_mixed_nodal(int n, const TreeDev &t, const double *nodeMB, const dbl
         k_mixed_nodal<<<blocks(n, 256), 256, 0, st>>>(n, t, nodeMB, ptXA, ptMB, ptDM, ptDMl, pStride);
 }
 
+__global__ void k_replay_records(int nNodes, const float *nodeDC, const float *nodeDn, float4 *rr) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nNodes) return;
+    float4 *r = rr + 8 * int64_t(q);
+    r[0].w = nodeDn[q];
+    const float4 *dc = reinterpret_cast<const float4 *>(nodeDC + 12 * int64_t(q));
+    // leaves (flag in r[5].x) keep their point range in r[1].w and r[2].x
+    if (__float_as_int(r[5].x) != 0) return;
+    r[2] = dc[0];
+    r[3] = dc[1];
+    r[4] = dc[2];
+}
+
+void launch_replay_records(int nNodes, const float *nodeDC, const float *nodeDn, float4 *rr, cudaStream_t st) {
+    if (nNodes > 0 && rr) k_replay_records<<<blocks(nNodes, 256), 256, 0, st>>>(nNodes, nodeDC, nodeDn, rr);
+}
+
 void launch_mixed_nodes(const TreeDev &t, const double *nodeMB, const double *ptMB, float *nodeDC, float *nodeDCl,
                         float *nodeDn, float *refDB, cudaStream_t st, int nStride, int dnStride) {
     if (t.nNodes > 0)
