@@ -628,7 +628,9 @@ def run_case(case, cfg, reps):
         for _ in range(reps):
             mesh.warpMesh()
     torch.cuda.synchronize()
-    print(json.dumps({"case": case, "config": cfg, "reps": reps, "lastKernelMs": mesh.getStats()["lastKernelMs"]}))
+    st = mesh.getStats()
+    print(json.dumps({"case": case, "config": cfg, "reps": reps, "lastKernelMs": st["lastKernelMs"],
+                      "walkListEntries": st["walkListEntries"]}))
     return 0
 
 
