@@ -161,6 +161,204 @@ __global__ void __launch_bounds__(kThreads) k_exact_mixed(TreeDevF tf, PointsDev
     cnt.flush(counters);
 }
 
+// k_exact_mixed for the default exponents (3, 5) with the volume nodes of a
+// thread taken two at a time in packed FP32 pairs (f32x2): each node's
+// arithmetic is leaf_pair's, rounding for rounding, so the sums stay bitwise
+// the walk's, while one instruction serves two nodes.  The staged points are
+// kept duplicated ((x, x, y, y) per float4), so every point operand of a pair
+// instruction comes straight from shared memory.
+constexpr int kTile2 = 128;  // surface points per shared-memory pass (static shared memory)
+
+template <int NV>
+__global__ void __launch_bounds__(kThreads) k_exact_mixed2(TreeDevF tf, PointsDevF pf, NodeAggF af, VolumeDev v,
+                                                           WalkRecF rec, MixedParams mp, Law32<0> law, float4 *acc,
+                                                           unsigned long long *counters) {
+    constexpr int NP = NV / 2;  // node pairs per thread
+    const int nPts = tf.nPts;
+    // per point: (dx, dx, dy, dy), (dz, dz, A, A), (lx, lx, ly, ly), (lz, lz, 0, 0), then D', u' in pairs
+    __shared__ float4 sP[10 * kTile2];
+    __shared__ float4 sRH[NV][kThreads], sRL[NV][kThreads];
+    const int tid = threadIdx.x;
+    const int64_t base = int64_t(blockIdx.x) * (kThreads * NV);
+    bool valid[NV];
+    int64_t g[NV];
+    float2 LS[NP], LSLO[NP], C1[NP];
+    float gv[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        const int64_t gid = base + j * kThreads + tid;
+        valid[j] = gid < v.nVol;
+        g[j] = valid[j] ? gid : 0;
+        const NodeScale ns = node_scale(rec, mp, g[j]);
+        if (j & 1) {
+            LS[j >> 1].y = ns.Ls;
+            LSLO[j >> 1].y = ns.LsLo;
+            C1[j >> 1].y = ns.c1;
+        } else {
+            LS[j >> 1].x = ns.Ls;
+            LSLO[j >> 1].x = ns.LsLo;
+            C1[j >> 1].x = ns.c1;
+        }
+        gv[j] = ns.gv;
+    }
+    const float2 AB = dup2(mp.abH), ABL = dup2(mp.abL), EPS = dup2(1e-15f);
+    MixedCounters cnt;
+    for (int kk = 0; kk < mp.nLoop; ++kk) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            sRH[j][tid] = rec.hi[kk * v.nVol + g[j]];
+            sRL[j][tid] = rec.lo[kk * v.nVol + g[j]];
+        }
+        float sn[NV][3], cn[NV][3], sd[NV], cd[NV];
+        float2 H[NP][3], Lw[NP][3], PN[NP][3], PD[NP];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            sd[j] = cd[j] = 0.f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) sn[j][a] = cn[j][a] = 0.f;
+        }
+#pragma unroll
+        for (int jj = 0; jj < NP; ++jj) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) H[jj][a] = Lw[jj][a] = PN[jj][a] = make_float2(0.f, 0.f);
+            PD[jj] = make_float2(0.f, 0.f);
+        }
+        int leaf = 0;
+        int4 L = tf.leaves[0];  // (l, u, node): the leaf in progress
+        for (int p0 = 0; p0 < nPts; p0 += kTile2) {
+            const int p1 = min(nPts, p0 + kTile2);
+            __syncthreads();
+            for (int q = tid; q < p1 - p0; q += kThreads) {
+                const float4 da = ldgf4(pf.da + p0 + q), dl = ldgf4(pf.dl + p0 + q);
+                const float4 *dmp = reinterpret_cast<const float4 *>(pf.dm) + 3 * int64_t(p0 + q);
+                const float4 m0 = ldgf4(dmp), m1 = ldgf4(dmp + 1), m2 = ldgf4(dmp + 2);
+                float4 *o = sP + 10 * q;
+                o[0] = make_float4(da.x, da.x, da.y, da.y);
+                o[1] = make_float4(da.z, da.z, da.w, da.w);
+                o[2] = make_float4(dl.x, dl.x, dl.y, dl.y);
+                o[3] = make_float4(dl.z, dl.z, 0.f, 0.f);
+                o[4] = make_float4(m0.x, m0.x, m0.y, m0.y);
+                o[5] = make_float4(m0.z, m0.z, m0.w, m0.w);
+                o[6] = make_float4(m1.x, m1.x, m1.y, m1.y);
+                o[7] = make_float4(m1.z, m1.z, m1.w, m1.w);
+                o[8] = make_float4(m2.x, m2.x, m2.y, m2.y);
+                o[9] = make_float4(m2.z, m2.z, m2.w, m2.w);
+            }
+            __syncthreads();
+            int p = p0;
+            while (p < p1) {
+                if (p == L.x) {
+                    // leaf start: r - C as hi + lo (exact high parts)
+                    const float4 ch = ldgf4(&tf.nodes[L.z].cHi), cl = ldgf4(&tf.nodes[L.z].cLo);
+#pragma unroll
+                    for (int j = 0; j < NV; ++j) {
+                        const float4 rh = sRH[j][tid], rl = sRL[j][tid];
+                        float hh[3], ll[3];
+                        two_diff(rh.x, ch.x, hh[0], ll[0]);
+                        two_diff(rh.y, ch.y, hh[1], ll[1]);
+                        two_diff(rh.z, ch.z, hh[2], ll[2]);
+                        ll[0] += rl.x - cl.x;
+                        ll[1] += rl.y - cl.y;
+                        ll[2] += rl.z - cl.z;
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            if (j & 1) {
+                                H[j >> 1][a].y = hh[a];
+                                Lw[j >> 1][a].y = ll[a];
+                            } else {
+                                H[j >> 1][a].x = hh[a];
+                                Lw[j >> 1][a].x = ll[a];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int jj = 0; jj < NP; ++jj) {
+                        PN[jj][0] = PN[jj][1] = PN[jj][2] = PD[jj] = make_float2(0.f, 0.f);
+                    }
+                }
+                const int e = min(L.y + 1, p1);
+                for (int q = p - p0; q < e - p0; ++q) {
+                    const float4 *o = sP + 10 * q;
+                    const float4 a0 = o[0], a1 = o[1], l0 = o[2], l1 = o[3];
+                    const float4 d0 = o[4], d1 = o[5], d2 = o[6], d3 = o[7], d4 = o[8], d5 = o[9];
+#pragma unroll
+                    for (int jj = 0; jj < NP; ++jj) {
+                        // leaf_pair for two nodes
+                        const float2 dx = add2(sub2(H[jj][0], lo2(a0)), sub2(Lw[jj][0], lo2(l0)));
+                        const float2 dy = add2(sub2(H[jj][1], hi2(a0)), sub2(Lw[jj][1], hi2(l0)));
+                        const float2 dz = add2(sub2(H[jj][2], lo2(a1)), sub2(Lw[jj][2], lo2(l1)));
+                        const float2 q2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, EPS)));
+                        const float2 r1 = make_float2(rsqrt_normal(q2.x), rsqrt_normal(q2.y));
+                        const float2 tt = fma2(LS[jj], r1, mul2(LSLO[jj], r1));
+                        const float2 t2 = mul2(tt, tt);
+                        const float2 t3 = mul2(t2, tt);
+                        const float2 t5 = mul2(t3, t2);
+                        const float2 lw = fma2(C1[jj], t3, fma2(AB, t5, mul2(ABL, t5)));
+                        const float2 w = mul2(hi2(a1), lw);
+                        const float2 S0 = fma2(lo2(d0), dx, fma2(hi2(d0), dy, fma2(lo2(d1), dz, hi2(d4))));
+                        const float2 S1 = fma2(hi2(d1), dx, fma2(lo2(d2), dy, fma2(hi2(d2), dz, lo2(d5))));
+                        const float2 S2 = fma2(lo2(d3), dx, fma2(hi2(d3), dy, fma2(lo2(d4), dz, hi2(d5))));
+                        PN[jj][0] = fma2(w, S0, PN[jj][0]);
+                        PN[jj][1] = fma2(w, S1, PN[jj][1]);
+                        PN[jj][2] = fma2(w, S2, PN[jj][2]);
+                        PD[jj] = add2(PD[jj], w);
+                    }
+                }
+                p = e;
+                if (e == L.y + 1) {
+                    // leaf end: gate, compensated sums, heavy leaves in double-float
+                    const float dn = __ldg(af.dn + L.z);
+                    const unsigned size = unsigned(L.y - L.x + 1);
+                    unsigned precisePairs = 0;
+#pragma unroll
+                    for (int j = 0; j < NV; ++j) {
+                        const int jj = j >> 1;
+                        const bool odd = j & 1;
+                        const bool prec = leaf_close<0>(
+                            odd ? PN[jj][0].y : PN[jj][0].x, odd ? PN[jj][1].y : PN[jj][1].x,
+                            odd ? PN[jj][2].y : PN[jj][2].x, odd ? PD[jj].y : PD[jj].x, dn, odd ? H[jj][0].y : H[jj][0].x,
+                            odd ? H[jj][1].y : H[jj][1].x, odd ? H[jj][2].y : H[jj][2].x, gv[j], sn[j], cn[j], sd[j],
+                            cd[j]);
+                        if (valid[j]) {
+                            cnt.leafPairs += size;
+                            cnt.visited++;
+                        }
+                        if (prec && valid[j]) {
+                            const float4 rh = sRH[j][tid], rl = sRL[j][tid];
+                            const float rhv[3] = {rh.x, rh.y, rh.z}, rlv[3] = {rl.x, rl.y, rl.z};
+                            const float Lsj = odd ? LS[jj].y : LS[jj].x, LsLoj = odd ? LSLO[jj].y : LSLO[jj].x,
+                                        c1j = odd ? C1[jj].y : C1[jj].x;
+                            precise_leaf<0>(tf, pf, L.z, L.x, L.y, rhv, rlv, law, Lsj, LsLoj, c1j, mp.abH, mp.abL,
+                                            sn[j], cn[j], sd[j], cd[j]);
+                            precisePairs += size;
+                        }
+                    }
+                    if (__any_sync(kFull, precisePairs != 0)) warp_count(counters, 6, precisePairs);
+                    ++leaf;
+                    if (leaf < tf.nLeaves) L = tf.leaves[leaf];
+                }
+            }
+        }
+        // the mirror's sums into the running pair (acc, the walk's layout)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            const float4 rh = sRH[j][tid], rl = sRL[j][tid];
+            const float rhv[3] = {rh.x, rh.y, rh.z}, rlv[3] = {rl.x, rl.y, rl.z};
+            float4 S4 = make_float4(0.f, 0.f, 0.f, 0.f), C4 = S4;
+            if (kk > 0 && valid[j]) {
+                S4 = acc[2 * g[j]];
+                C4 = acc[2 * g[j] + 1];
+            }
+            finish_mirror(af, mp, kk, rhv, rlv, sn[j], cn[j], sd[j], cd[j], S4, C4);
+            if (valid[j]) {
+                acc[2 * g[j]] = S4;
+                acc[2 * g[j] + 1] = C4;
+            }
+        }
+    }
+    cnt.flush(counters);
+}
+
 // Exact-mode reverse product for one seed (evalNodeExact_b on the root,
 // kd_tree.F90:942-1031, driven as warpDeriv.F90:71-88): every pair's weight
 // as in the forward kernel, times the node's seed numb = dXv / den (reflected
@@ -296,6 +494,15 @@ template <int KIND>
 void launch_kind(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, const VolumeDev &v,
                  const WalkRecF &rec, const MixedParams &mp, const Law32<KIND> &law, float4 *acc,
                  unsigned long long *counters, cudaStream_t st) {
+    if constexpr (KIND == 0) {
+        if (blocks_for(v.nVol, kThreads * 4) >= sm_count() * kBlocksPerSmNV4)
+            k_exact_mixed2<4><<<blocks_for(v.nVol, kThreads * 4), kThreads, 0, st>>>(tf, pf, af, v, rec, mp, law, acc,
+                                                                                    counters);
+        else
+            k_exact_mixed2<2><<<blocks_for(v.nVol, kThreads * 2), kThreads, 0, st>>>(tf, pf, af, v, rec, mp, law, acc,
+                                                                                    counters);
+        return;
+    }
     if (blocks_for(v.nVol, kThreads * 4) >= sm_count() * kBlocksPerSmNV4)
         k_exact_mixed<KIND, 4><<<blocks_for(v.nVol, kThreads * 4), kThreads, 0, st>>>(tf, pf, af, v, rec, mp, law,
                                                                                      acc, counters);

@@ -70,6 +70,10 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 // scalar results bit for bit with one instruction issued for two.
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
     unsigned long long d;
     asm("sub.rn.f32x2 %0, %1, %2;"
