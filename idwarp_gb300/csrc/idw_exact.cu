@@ -209,19 +209,15 @@ __global__ void __launch_bounds__(kThreads) k_exact_mixed2(TreeDevF tf, PointsDe
             sRH[j][tid] = rec.hi[kk * v.nVol + g[j]];
             sRL[j][tid] = rec.lo[kk * v.nVol + g[j]];
         }
-        float sn[NV][3], cn[NV][3], sd[NV], cd[NV];
+        // running compensated sums (numerator 3, denominator) of the node pairs
+        float2 SN[NP][3], CN[NP][3], SD[NP], CD[NP];
         float2 H[NP][3], Lw[NP][3], PN[NP][3], PD[NP];
-#pragma unroll
-        for (int j = 0; j < NV; ++j) {
-            sd[j] = cd[j] = 0.f;
-#pragma unroll
-            for (int a = 0; a < 3; ++a) sn[j][a] = cn[j][a] = 0.f;
-        }
 #pragma unroll
         for (int jj = 0; jj < NP; ++jj) {
 #pragma unroll
-            for (int a = 0; a < 3; ++a) H[jj][a] = Lw[jj][a] = PN[jj][a] = make_float2(0.f, 0.f);
-            PD[jj] = make_float2(0.f, 0.f);
+            for (int a = 0; a < 3; ++a)
+                SN[jj][a] = CN[jj][a] = H[jj][a] = Lw[jj][a] = PN[jj][a] = make_float2(0.f, 0.f);
+            SD[jj] = CD[jj] = PD[jj] = make_float2(0.f, 0.f);
         }
         int leaf = 0;
         int4 L = tf.leaves[0];  // (l, u, node): the leaf in progress
@@ -311,26 +307,66 @@ __global__ void __launch_bounds__(kThreads) k_exact_mixed2(TreeDevF tf, PointsDe
                     const unsigned size = unsigned(L.y - L.x + 1);
                     unsigned precisePairs = 0;
 #pragma unroll
-                    for (int j = 0; j < NV; ++j) {
-                        const int jj = j >> 1;
-                        const bool odd = j & 1;
-                        const bool prec = leaf_close<0>(
-                            odd ? PN[jj][0].y : PN[jj][0].x, odd ? PN[jj][1].y : PN[jj][1].x,
-                            odd ? PN[jj][2].y : PN[jj][2].x, odd ? PD[jj].y : PD[jj].x, dn, odd ? H[jj][0].y : H[jj][0].x,
-                            odd ? H[jj][1].y : H[jj][1].x, odd ? H[jj][2].y : H[jj][2].x, gv[j], sn[j], cn[j], sd[j],
-                            cd[j]);
-                        if (valid[j]) {
-                            cnt.leafPairs += size;
-                            cnt.visited++;
+                    for (int jj = 0; jj < NP; ++jj) {
+                        // leaf_close for the pair: the gate per node, the
+                        // compensated adds packed (bitwise kahan_add per node)
+                        const bool pa = leaf_gate_mag(PN[jj][0].x, PN[jj][1].x, PN[jj][2].x, PD[jj].x, dn,
+                                                      H[jj][0].x, H[jj][1].x, H[jj][2].x) > gv[2 * jj];
+                        const bool pb = leaf_gate_mag(PN[jj][0].y, PN[jj][1].y, PN[jj][2].y, PD[jj].y, dn,
+                                                      H[jj][0].y, H[jj][1].y, H[jj][2].y) > gv[2 * jj + 1];
+                        if (!pa && !pb) {
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) kahan_add2(SN[jj][a], CN[jj][a], PN[jj][a]);
+                            kahan_add2(SD[jj], CD[jj], PD[jj]);
+                        } else {
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) {
+                                if (!pa) kahan_add(SN[jj][a].x, CN[jj][a].x, PN[jj][a].x);
+                                if (!pb) kahan_add(SN[jj][a].y, CN[jj][a].y, PN[jj][a].y);
+                            }
+                            if (!pa) kahan_add(SD[jj].x, CD[jj].x, PD[jj].x);
+                            if (!pb) kahan_add(SD[jj].y, CD[jj].y, PD[jj].y);
                         }
-                        if (prec && valid[j]) {
-                            const float4 rh = sRH[j][tid], rl = sRL[j][tid];
-                            const float rhv[3] = {rh.x, rh.y, rh.z}, rlv[3] = {rl.x, rl.y, rl.z};
-                            const float Lsj = odd ? LS[jj].y : LS[jj].x, LsLoj = odd ? LSLO[jj].y : LSLO[jj].x,
-                                        c1j = odd ? C1[jj].y : C1[jj].x;
-                            precise_leaf<0>(tf, pf, L.z, L.x, L.y, rhv, rlv, law, Lsj, LsLoj, c1j, mp.abH, mp.abL,
-                                            sn[j], cn[j], sd[j], cd[j]);
-                            precisePairs += size;
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int j = 2 * jj + h;
+                            if (valid[j]) {
+                                cnt.leafPairs += size;
+                                cnt.visited++;
+                            }
+                            if ((h ? pb : pa) && valid[j]) {
+                                const float4 rh = sRH[j][tid], rl = sRL[j][tid];
+                                const float rhv[3] = {rh.x, rh.y, rh.z}, rlv[3] = {rl.x, rl.y, rl.z};
+                                float sn[3], cn[3], sd, cd;
+#pragma unroll
+                                for (int a = 0; a < 3; ++a) {
+                                    sn[a] = h ? SN[jj][a].y : SN[jj][a].x;
+                                    cn[a] = h ? CN[jj][a].y : CN[jj][a].x;
+                                }
+                                sd = h ? SD[jj].y : SD[jj].x;
+                                cd = h ? CD[jj].y : CD[jj].x;
+                                precise_leaf<0>(tf, pf, L.z, L.x, L.y, rhv, rlv, law, h ? LS[jj].y : LS[jj].x,
+                                                h ? LSLO[jj].y : LSLO[jj].x, h ? C1[jj].y : C1[jj].x, mp.abH,
+                                                mp.abL, sn, cn, sd, cd);
+#pragma unroll
+                                for (int a = 0; a < 3; ++a) {
+                                    if (h) {
+                                        SN[jj][a].y = sn[a];
+                                        CN[jj][a].y = cn[a];
+                                    } else {
+                                        SN[jj][a].x = sn[a];
+                                        CN[jj][a].x = cn[a];
+                                    }
+                                }
+                                if (h) {
+                                    SD[jj].y = sd;
+                                    CD[jj].y = cd;
+                                } else {
+                                    SD[jj].x = sd;
+                                    CD[jj].x = cd;
+                                }
+                                precisePairs += size;
+                            }
                         }
                     }
                     if (__any_sync(kFull, precisePairs != 0)) warp_count(counters, 6, precisePairs);
@@ -349,7 +385,14 @@ __global__ void __launch_bounds__(kThreads) k_exact_mixed2(TreeDevF tf, PointsDe
                 S4 = acc[2 * g[j]];
                 C4 = acc[2 * g[j] + 1];
             }
-            finish_mirror(af, mp, kk, rhv, rlv, sn[j], cn[j], sd[j], cd[j], S4, C4);
+            const int jj = j >> 1;
+            const bool odd = j & 1;
+            const float snj[3] = {odd ? SN[jj][0].y : SN[jj][0].x, odd ? SN[jj][1].y : SN[jj][1].x,
+                                  odd ? SN[jj][2].y : SN[jj][2].x};
+            const float cnj[3] = {odd ? CN[jj][0].y : CN[jj][0].x, odd ? CN[jj][1].y : CN[jj][1].x,
+                                  odd ? CN[jj][2].y : CN[jj][2].x};
+            finish_mirror(af, mp, kk, rhv, rlv, snj, cnj, odd ? SD[jj].y : SD[jj].x, odd ? CD[jj].y : CD[jj].x, S4,
+                          C4);
             if (valid[j]) {
                 acc[2 * g[j]] = S4;
                 acc[2 * g[j] + 1] = C4;

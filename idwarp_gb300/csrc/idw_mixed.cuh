@@ -477,6 +477,14 @@ __device__ __forceinline__ void leaf_pair(const Law32<KIND> &law, float Ls, floa
     pd += w;
 }
 
+// The leaf gate's measure: the leaf's FP32 partial sums bound the rounding
+// of its terms, pd |D'| |r - C| that of the lever arm (all forms share it,
+// so their gates decide alike).
+__device__ __forceinline__ float leaf_gate_mag(float pn0, float pn1, float pn2, float pd, float dn, float h0,
+                                               float h1, float h2) {
+    return fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + pd * dn * (fabsf(h0) + fabsf(h1) + fabsf(h2));
+}
+
 // End of a leaf: its partial sums go into the compensated running sums,
 // unless the leaf carries a large weight at a long lever arm (the cluster
 // terms' gate, with dn the leaf's bound on |D'|); returns true for such a
@@ -484,8 +492,7 @@ __device__ __forceinline__ void leaf_pair(const Law32<KIND> &law, float Ls, floa
 template <int KIND>
 __device__ __forceinline__ bool leaf_close(float pn0, float pn1, float pn2, float pd, float dn, float h0, float h1,
                                            float h2, float gv, float *sn, float *cn, float &sd, float &cd) {
-    const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + pd * dn * (fabsf(h0) + fabsf(h1) + fabsf(h2));
-    const bool precise = KIND != 2 && lmag > gv;
+    const bool precise = KIND != 2 && leaf_gate_mag(pn0, pn1, pn2, pd, dn, h0, h1, h2) > gv;
     if (!precise) {
         kahan_add(sn[0], cn[0], pn0);
         kahan_add(sn[1], cn[1], pn1);
@@ -499,8 +506,7 @@ __device__ __forceinline__ bool leaf_close(float pn0, float pn1, float pn2, floa
 template <int KIND>
 __device__ __forceinline__ bool leaf_close2(float pn0, float pn1, float pn2, float pd, float dn, float h0, float h1,
                                             float h2, float gv, Sums2 &r) {
-    const float lmag = fabsf(pn0) + fabsf(pn1) + fabsf(pn2) + pd * dn * (fabsf(h0) + fabsf(h1) + fabsf(h2));
-    const bool precise = KIND != 2 && lmag > gv;
+    const bool precise = KIND != 2 && leaf_gate_mag(pn0, pn1, pn2, pd, dn, h0, h1, h2) > gv;
     if (!precise) {
         kahan_add2(r.s01, r.c01, make_float2(pn0, pn1));
         kahan_add2(r.s2d, r.c2d, make_float2(pn2, pd));
