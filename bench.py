@@ -817,8 +817,9 @@ def main():
                 "max_diff_between_step_outputs": e2e_check},
         "clocks": clk,
         # per step: gather_xu, face_props, nodal, set_data, mixed_nodal,
-        # mixed_nodes, walk, finalize (+ the replay's counter add)
-        "gpu_launches": (9 if st["walkListEntries"] > 0 else 8) * args.steps,
+        # mixed_nodes, walk, finalize (+ the replay's record refresh and
+        # counter add)
+        "gpu_launches": (10 if st["walkListEntries"] > 0 else 8) * args.steps,
         "setup_s": setup_s,
         "first_warp_s": first_warp_s,
         "walk_lists": {"entries": st["walkListEntries"], "bytes": 8 * max(0, st["walkListEntries"]),
