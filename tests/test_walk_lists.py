@@ -164,3 +164,27 @@ def test_reverse_product_replay(prec, nseeds, built_lib):
     assert np.abs(res[0][0] - res[1][0]).max() <= 1e-11 * scale
     for k in ("leafPairs", "approx", "visited", "fp64Fallback"):
         assert res[0][1][k] == res[1][1][k], k
+
+
+def test_new_estimate_rerecords(built_lib):
+    # a denominator estimate loaded after the first warp (as from a restart
+    # file) moves every decision threshold: the lists are recorded again
+    import ctypes as C
+
+    from idwarp_gb300 import _lib
+
+    m = wing_small()
+    res = []
+    for wl in ("auto", "off"):
+        g = build_gpu(m, {"walkLists": wl}, precision="mixed")
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        s0 = g.getStats()
+        den = np.ascontiguousarray(g.getDenominator0() * 3.0)
+        assert g.lib.idw_set_denominator0(g.ctx, den.ctypes.data_as(C.c_void_p), len(den), 0, _lib.IDW_HOST) == 0
+        g.warpMesh()
+        res.append((g.getWarpGrid().copy(), g.getStats(), s0))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    for k in STATS:
+        assert res[0][1][k] == res[1][1][k], k
+    assert res[0][1]["approx"] != res[0][2]["approx"]
