@@ -56,12 +56,13 @@ def make_workload(cfg, seed=2):
 
 
 WALK_LISTS = "auto"  # --walk-lists: "off" makes every walk decide as it goes
+TREE_BUILD = "kd"  # --tree-build: "morton" builds the surface tree on the GPU
 
 
-def mesh_options(m, precision, mode="fast"):
+def mesh_options(m, precision, mode="fast", tree=None):
     return {"fileType": "NPY", "precision": precision, "evalMode": mode, "errTol": ERR_TOL,
             "aExp": 3.0, "bExp": 5.0, "LdefFact": 1.0, "alpha": 0.25, "bucketSize": 8,
-            "symmetryPlanes": m["symmetryPlanes"], "walkLists": WALK_LISTS}
+            "symmetryPlanes": m["symmetryPlanes"], "walkLists": WALK_LISTS, "treeBuild": tree or TREE_BUILD}
 
 
 def build_mesh(m, precision, mode="fast", restartFile=None):
@@ -192,7 +193,8 @@ def workload_config(cfg, m, mode, nunique, world):
     nvol = len(m["xv0"])
     return {"workload": "wing_shell_%dx%dx%d" % CONFIGS[cfg], "volume_nodes": nvol, "surface_points": len(m["pts"]),
             "unique_surface_nodes": int(nunique), "errTol": ERR_TOL, "mode": mode,
-            "symmetry_planes": len(m["symmetryPlanes"]), "parallelism": "replicas" if world > 1 else "single",
+            "symmetry_planes": len(m["symmetryPlanes"]), "surface_tree": TREE_BUILD,
+            "parallelism": "replicas" if world > 1 else "single",
             "l2": "inputs %s L2 (Xv0+Xv+den0+den ~%.0f MB per step)" % (
                 "larger than" if nvol * 64 > 129e6 else "fit in", nvol * 64 / 1e6)}
 
@@ -202,13 +204,13 @@ class OracleSample:
     of the workload's volume nodes: the volume nodes are independent given
     the surface, so a sample is a bounded piece of the same work."""
 
-    def __init__(self, m, idx, library=None, mode="fast"):
+    def __init__(self, m, idx, library=None, mode="fast", tree="kd"):
         from oracle.pyoracle import OracleMesh
 
-        o = dict(mesh_options(m, "fp64", mode))
+        o = dict(mesh_options(m, "fp64", mode, tree))
         self.idx = idx
         self.om = OracleMesh({k: o[k] for k in ("aExp", "bExp", "LdefFact", "alpha", "errTol", "evalMode",
-                                                "bucketSize")}, library=library)
+                                                "bucketSize", "treeBuild")}, library=library)
         self.om.set_volume(m["xv0"][idx])
         planes = m["symmetryPlanes"]
         self.om.set_symmetry(np.array([p[0] for p in planes]).reshape(-1, 3),
@@ -273,15 +275,16 @@ def run_parity(m, idx, xv_timing, grids, gpu_stats_fn):
     the sampled nodes give the GPU's decision counts for the same nodes.
     The timing build's difference from the checker is the case's rounding
     sensitivity (different rounding order of the same formulas)."""
-    s = OracleSample(m, idx)
+    s = OracleSample(m, idx, tree=TREE_BUILD)
     xo = s.step()
     ost = s.om.stats()
     L = s.om.ldef0()
-    out = {"n_nodes": int(len(idx)), "sample": "the CPU baseline's sample", "Ldef": L,
+    # the timing build runs the reference's kd tree: a rounding comparison only on that tree
+    sens = float(np.abs(xv_timing - xo).max() / L) if TREE_BUILD == "kd" else 0.0
+    out = {"n_nodes": int(len(idx)), "sample": "the CPU baseline's sample", "Ldef": L, "surface_tree": TREE_BUILD,
            "oracle": {"leafPairs": ost["leafPairs"], "approx": ost["approx"]},
-           "rounding_sensitivity_over_Ldef": float(np.abs(xv_timing - xo).max() / L)}
+           "rounding_sensitivity_over_Ldef": sens if TREE_BUILD == "kd" else None}
     del s
-    sens = out["rounding_sensitivity_over_Ldef"]
     ok = True
     for prec, bar in (("mixed", 1e-8), ("fp64", 1e-12)):
         st = gpu_stats_fn(prec, idx)
@@ -480,6 +483,80 @@ def run_suite():
     return 0
 
 
+def run_suite_tree():
+    """Error report of the Morton tree (treeBuild "morton", built on the GPU)
+    against the reference kd tree, one JSON line per mesh and errTol: set-up
+    and tree build times, tree shape, the mixed fast walk (first warp, which
+    records its decisions, and the replayed steady state), its work, and its
+    error against mixed exact mode (max and RMS of |dx| / Ldef0 over every
+    volume node)."""
+    import torch
+
+    from idwarp_gb300 import USMesh
+    from idwarp_gb300 import _lib
+    from idwarp_gb300 import synthetic as S
+
+    stream = torch.cuda.current_stream()
+
+    def gpu_mesh(m, mode, errTol, tree):
+        o = mesh_options(m, "mixed", mode, tree)
+        o["errTol"] = errTol
+        t0 = time.perf_counter()
+        with contextlib.redirect_stdout(io.StringIO()):
+            g = USMesh(o)
+            g.createCommonGrid(m["xv0"])
+            g.setSurfaceDefinition(m["pts"], m["conn"], m["faceSizes"])
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        g.lib.idw_set_stream(g.ctx, C.c_void_p(stream.cuda_stream))
+        return g, setup
+
+    sph = S.sphere_ogrid(n=18, layers=48)
+    sph["xs"] = S.sphere_perturbation(sph["pts"], seed=0)
+    rows = [("S1_sphere_95k", sph, [1e-4]), ("W_wing_2M", make_workload("W"), [1e-3, 1e-4, 1e-5]),
+            ("P_wing_8M", make_workload("P"), [1e-4])]
+    for name, m, tols in rows:
+        nvol = len(m["xv0"])
+        xs_dev = torch.tensor(m["xs"], dtype=torch.float64, device="cuda")
+
+        def step(g):
+            g.lib.idw_set_surface_coordinates(g.ctx, C.c_void_p(xs_dev.data_ptr()), xs_dev.numel(), _lib.IDW_DEVICE)
+            g.lib.idw_warp_mesh(g.ctx)
+
+        ge, _ = gpu_mesh(m, "exact", 1e-4, "kd")
+        exact_ms = _timed(lambda: step(ge), 1, stream)
+        xe = ge.getWarpGrid().reshape(-1, 3).copy()
+        L = ge.getStats()["Ldef0"]
+        del ge
+        for errTol in tols:
+            res = {"row": name, "volume_nodes": nvol, "surface_points": len(m["pts"]), "errTol": errTol,
+                   "exact_mixed_ms": exact_ms}
+            for tree in ("kd", "morton"):
+                g, setup = gpu_mesh(m, "fast", errTol, tree)
+                st = g.getStats()
+                t = g.getTree()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                step(g)
+                torch.cuda.synchronize()
+                first = time.perf_counter() - t0
+                ms = _timed(lambda: step(g), 5, stream)
+                st2 = g.getStats()
+                e = np.abs(g.getWarpGrid().reshape(-1, 3) - xe).max(axis=1) / L
+                res.update({
+                    "%s_setup_s" % tree: setup, "%s_tree_build_ms" % tree: st["treeBuildMs"],
+                    "%s_tree_nodes" % tree: int(st["nTreeNodes"]), "%s_leaves" % tree: int(t["isLeaf"].sum()),
+                    "%s_max_depth" % tree: int(st["maxDepth"]), "%s_first_warp_ms" % tree: 1e3 * first,
+                    "%s_warp_ms" % tree: ms, "%s_nodes_per_s" % tree: nvol / (ms * 1e-3),
+                    "%s_leafPairs_per_node" % tree: st2["leafPairs"] / nvol,
+                    "%s_approx_per_node" % tree: st2["approx"] / nvol,
+                    "%s_vs_exact_max_over_Ldef" % tree: float(e.max()),
+                    "%s_vs_exact_rms_over_Ldef" % tree: float(np.sqrt(np.mean(e ** 2)))})
+                del g
+            print(json.dumps(res), flush=True)
+    return 0
+
+
 def run_suite_d(steps=50, sample=200000, directions=5):
     """Differentiation at scale: the two-body mesh (wing 577x261x53 + sphere
     158x79: 19.96M volume nodes, 302k surface points), 50 Adam steps on 48
@@ -565,7 +642,7 @@ def run_suite_d(steps=50, sample=200000, directions=5):
     t0 = time.perf_counter()
     smp = dict(m)
     smp["xs"] = xs.cpu().numpy()
-    ors = OracleSample(smp, idx)
+    ors = OracleSample(smp, idx, tree=TREE_BUILD)
     ors.step()
     dxs_or = ors.om.warp_deriv(gs[idx])
     res["oracle_seconds"] = time.perf_counter() - t0
@@ -647,22 +724,29 @@ def main():
                     help="evalMode of the timed warp; the extra measurements and the CPU baseline are fast-mode only")
     ap.add_argument("--suite", action="store_true", help="measurement table rows (S1, W, P errTol sweep)")
     ap.add_argument("--suite-d", action="store_true", help="the 20M-node two-body FFD loop")
+    ap.add_argument("--suite-tree", action="store_true",
+                    help="error report of the GPU-built Morton tree against the kd tree (S1, W errTol sweep, P)")
+    ap.add_argument("--tree-build", default="kd", choices=["kd", "morton"],
+                    help="surface tree: the reference's kd tree (host) or the Morton tree (GPU)")
     ap.add_argument("--walk-lists", default="auto", choices=["auto", "off"],
                     help="mixed fast mode: replay recorded walk decisions (auto) or decide in every walk (off)")
     ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "deriv16", "deriv16fast", "batch"],
                     help="run one operation --steps times on --config's mesh (the small profiling cases)")
     args = ap.parse_args()
-    global WALK_LISTS
+    global WALK_LISTS, TREE_BUILD
     WALK_LISTS = args.walk_lists
+    TREE_BUILD = args.tree_build
     if args.case:
         import torch
 
         torch.cuda.set_device(_env_int("LOCAL_RANK", 0))
         return run_case(args.case, args.config, args.steps)
-    if args.suite or args.suite_d:
+    if args.suite or args.suite_d or args.suite_tree:
         import torch
 
         torch.cuda.set_device(_env_int("LOCAL_RANK", 0))
+        if args.suite_tree:
+            return run_suite_tree()
         return run_suite() if args.suite else run_suite_d()
 
     rank = _env_int("RANK", 0)

@@ -104,6 +104,7 @@ class USMesh(BaseSolver):
             "exactSchedule": [str, ["auto", "tiled", "walk"]],
             "adjointPrecision": [str, ["precise", "fast"]],
             "walkLists": [str, ["auto", "off"]],
+            "treeBuild": [str, ["kd", "morton"]],
         }
 
     # ------------------------------------------------------------------
@@ -564,6 +565,7 @@ class USMesh(BaseSolver):
         o.exactSchedule = {"auto": 0, "tiled": 1, "walk": 2}[self.getOption("exactSchedule")]
         o.adjointPrecision = {"precise": _lib.IDW_ADJ_PRECISE, "fast": _lib.IDW_ADJ_FAST}[self.getOption("adjointPrecision")]
         o.walkLists = {"auto": _lib.IDW_WALK_LISTS_AUTO, "off": _lib.IDW_WALK_LISTS_OFF}[self.getOption("walkLists")]
+        o.treeBuild = {"kd": _lib.IDW_TREE_KD, "morton": _lib.IDW_TREE_MORTON}[self.getOption("treeBuild")]
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

@@ -20,6 +20,8 @@ IDW_ADJ_PRECISE = 0
 IDW_ADJ_FAST = 1
 IDW_WALK_LISTS_AUTO = 0
 IDW_WALK_LISTS_OFF = 1
+IDW_TREE_KD = 0
+IDW_TREE_MORTON = 1
 IDW_OK = 0
 IDW_ERR_ARG = -1
 IDW_ERR_STATE = -2
@@ -42,7 +44,7 @@ class idw_options(C.Structure):
         ("evalMode", C.c_int32), ("useRotations", C.c_int32), ("zeroCornerRotations", C.c_int32),
         ("bucketSize", C.c_int32), ("precision", C.c_int32), ("diagnostics", C.c_int32),
         ("mixedGate", C.c_double), ("exactSchedule", C.c_int32), ("adjointPrecision", C.c_int32),
-        ("walkLists", C.c_int32), ("reserved", C.c_int32 * 1),
+        ("walkLists", C.c_int32), ("treeBuild", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -52,7 +54,7 @@ class idw_stats(C.Structure):
         ("nUnique", C.c_int64), ("nTreeNodes", C.c_int64), ("maxDepth", C.c_int64), ("nVol", C.c_int64),
         ("nSurfPts", C.c_int64), ("nLoop", C.c_int64), ("Ldef0", C.c_double), ("lastKernelMs", C.c_double),
         ("warpLeafSlots", C.c_int64), ("warpNodeSlots", C.c_int64), ("preciseTerms", C.c_int64),
-        ("walkListEntries", C.c_int64),
+        ("walkListEntries", C.c_int64), ("treeBuildMs", C.c_double),
     ]
 
     def as_dict(self):

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libidwarp_gb300.so")
 
 SOURCES = ["idw_api.cu", "idw_walk.cu", "idw_mixed.cu", "idw_replay.cu", "idw_batch.cu", "idw_exact.cu", "idw_adjoint.cu", "idw_adjoint_precise.cu", "idw_nodal.cu", "idw_setup.cu",
-           "idw_probe.cu", "idw_complex.cu", "idw_host.cpp"]
+           "idw_tree.cu", "idw_probe.cu", "idw_complex.cu", "idw_host.cpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -276,6 +277,8 @@ int validate_options(Ctx *c, const idw_options *o) {
         return fail(c, IDW_ERR_ARG, "adjointPrecision must be IDW_ADJ_PRECISE or IDW_ADJ_FAST");
     if (o->walkLists != IDW_WALK_LISTS_AUTO && o->walkLists != IDW_WALK_LISTS_OFF)
         return fail(c, IDW_ERR_ARG, "walkLists must be IDW_WALK_LISTS_AUTO or IDW_WALK_LISTS_OFF");
+    if (o->treeBuild != IDW_TREE_KD && o->treeBuild != IDW_TREE_MORTON)
+        return fail(c, IDW_ERR_ARG, "treeBuild must be IDW_TREE_KD or IDW_TREE_MORTON");
     return IDW_OK;
 }
 
@@ -348,6 +351,7 @@ void idw_default_options(idw_options *o) {
     o->mixedGate = 2e-3;
     o->adjointPrecision = IDW_ADJ_PRECISE;
     o->walkLists = IDW_WALK_LISTS_AUTO;
+    o->treeBuild = IDW_TREE_KD;
 }
 
 int idw_create(const idw_options *opts, void **ctx_out) {
@@ -530,7 +534,15 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     c->haveTree = c->haveWarp = c->haveDxs = c->nodalValid = false;
 
     FlatTree t;
-    build_kdtree(uniquepts, nunique, c->opt.bucketSize, t);
+    const auto tTree = std::chrono::steady_clock::now();
+    if (c->opt.treeBuild == IDW_TREE_MORTON) {
+        const int rc = build_morton_tree(uniquepts, nunique, c->opt.bucketSize, t, c->stream);
+        if (rc == -2) return fail(c, IDW_ERR_NOMEM, "out of device memory in the surface tree build");
+        if (rc != 0) return fail(c, IDW_ERR_CUDA, "surface tree build: %s", cudaGetErrorString(cudaGetLastError()));
+    } else {
+        build_kdtree(uniquepts, nunique, c->opt.bucketSize, t);
+    }
+    const double treeMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tTree).count();
     const int n = nunique, nn = t.nodes();
     std::vector<int> inv(n);
     for (int i = 0; i < n; ++i) inv[t.perm[i]] = i;
@@ -740,6 +752,7 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     c->stats.nUnique = n;
     c->stats.nTreeNodes = nn;
     c->stats.maxDepth = t.maxDepth;
+    c->stats.treeBuildMs = treeMs;
     c->stats.nSurfPts = npts;
     c->stats.nLoop = c->sym.nLoop;
     c->stats.Ldef0 = L0;

@@ -271,4 +271,10 @@ int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDev
 int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
                 cudaStream_t st);
 
+// Surface tree built on the device (idw_tree.cu): Morton order, binary radix
+// tree cut at bucket-size leaves, in the host kd build's layout.  pts: host
+// array of n unique points.  0, -1 (CUDA error) or -2 (out of device memory).
+struct FlatTree;
+int build_morton_tree(const double *pts, int n, int bucket, FlatTree &t, cudaStream_t st);
+
 }  // namespace idw

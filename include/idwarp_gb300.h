@@ -60,6 +60,12 @@ extern "C" {
                                * (when the lists fit in half of the free device memory) */
 #define IDW_WALK_LISTS_OFF 1  /* every walk takes its decisions as it goes */
 
+#define IDW_TREE_KD 0     /* the reference's surface kd tree (build_tree, src/modules/kd_tree.F90:123-300),
+                           * built on the host: every fast-mode decision as the reference's */
+#define IDW_TREE_MORTON 1 /* binary radix tree over Morton-ordered surface points, built on the GPU and cut
+                           * at bucketSize+1 points; same aggregates, other clusters: fast-mode results
+                           * differ from the kd tree's within what errTol allows */
+
 /* Mesh options: the gridinput module variables (src/modules/gridInput.f90:9-18,
  * libidwarp.pyf:148-162) plus kd_tree.bucket_size (libidwarp.pyf:204-206) and
  * the GB300 precision switch.  Semantics follow doc/options.yaml. */
@@ -93,7 +99,9 @@ typedef struct idw_options {
                            * and errTol only, so they can be recorded once (per warp of 32
                            * volume nodes: the tree nodes where a lane approximates or sums
                            * a leaf) and replayed by every later warp; same sums either way */
-    int32_t reserved[1];
+    int32_t treeBuild;    /* IDW_TREE_KD (default) or IDW_TREE_MORTON; read by
+                           * idw_initialize_warping, as bucketSize */
+    int32_t reserved[3];
 } idw_options;
 
 /* Work counters of the last warp / warpDeriv call. */
@@ -114,6 +122,7 @@ typedef struct idw_stats {
     int64_t warpNodeSlots; /* lane slots of warp-level interior-node visits (32 per visit) */
     int64_t preciseTerms;  /* mixed mode: cluster terms summed in double-float */
     int64_t walkListEntries; /* recorded walk decisions (8 bytes each; -1: too large, walks decide) */
+    double treeBuildMs;   /* host wall time of the last surface tree build (kd or Morton, with its copies) */
 } idw_stats;
 
 /* Fill `o` with the reference defaults (idwarp/UnstructuredMesh.py:124-145). */

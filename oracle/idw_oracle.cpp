@@ -51,6 +51,7 @@ struct Opts {
     double aExp, bExp, LdefFact, alpha, errTol, cornerAngle;
     int evalMode;  // 0 exact, 1 fast (src/modules/gridInput.f90:16-17)
     int useRotations, zeroCornerRotations, bucketSize;
+    int treeBuild;  // 0: the reference's kd tree; 1: the library's Morton tree (no reference counterpart)
 };
 
 // src/modules/kd_tree.F90:63-79 (tree_node)
@@ -220,6 +221,109 @@ static int build_range(Tree &tp, int l, int u, int bucket) {
         tp.nodes[id].right = right;
     }
     return id;
+}
+
+// ---------------------------------------------------------------------------
+// Morton tree: the library's treeBuild "morton" option, which has no
+// counterpart in the reference.  Restated here from its definition, top-down,
+// to check the device build (which forms the same tree bottom-up in parallel):
+// points ordered by 63-bit Morton code (21 bits per axis over the bounding
+// cube, x in the highest bit of each triple; ties keep the point order); the
+// binary radix tree of the keys (code, index), whose node over [l, u] splits
+// after the last key sharing more than the common prefix of keys l and u;
+// leaves where u - l <= bucketSize; centroid sums bottom-up (a leaf's points
+// in order, an interior node's as left + right); radius as setCenters.
+// ---------------------------------------------------------------------------
+static void morton_order(const double *pts, int n, std::vector<unsigned long long> &codes, std::vector<int> &order) {
+    double lo[3], hi[3];
+    for (int c = 0; c < 3; ++c) lo[c] = hi[c] = pts[c];
+    for (int i = 1; i < n; ++i)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = std::min(lo[c], pts[3 * i + c]);
+            hi[c] = std::max(hi[c], pts[3 * i + c]);
+        }
+    const double ext = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    const double inv = ext > 0.0 ? 2097152.0 / ext : 0.0;
+    std::vector<unsigned long long> code(n);
+    for (int i = 0; i < n; ++i) {
+        unsigned q[3];
+        for (int c = 0; c < 3; ++c) {
+            const double f = std::floor((pts[3 * i + c] - lo[c]) * inv);
+            q[c] = f >= 2097151.0 ? 2097151u : unsigned(f);
+        }
+        unsigned long long k = 0;
+        for (int b = 0; b < 21; ++b)
+            for (int c = 0; c < 3; ++c) k |= (unsigned long long)((q[c] >> b) & 1u) << (3 * b + 2 - c);
+        code[i] = k;
+    }
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+    codes.resize(n);
+    for (int i = 0; i < n; ++i) codes[i] = code[order[i]];
+}
+
+// common prefix of the keys (code, position) at sorted positions i != j
+static int morton_prefix(const std::vector<unsigned long long> &k, int i, int j) {
+    if (k[i] != k[j]) return __builtin_clzll(k[i] ^ k[j]);
+    return 64 + __builtin_clz(unsigned(i ^ j));
+}
+
+static int build_morton_range(Tree &tp, const std::vector<unsigned long long> &k, int l, int u, int bucket) {
+    int id = int(tp.nodes.size());
+    tp.nodes.push_back(Node());
+    Node nd;
+    std::memset(&nd, 0, sizeof(nd));
+    nd.l = l;
+    nd.u = u;
+    nd.n = u - l + 1;
+    nd.left = nd.right = -1;
+    if ((u - l) <= bucket) {
+        nd.dnum = 0;
+        tp.nodes[id] = nd;
+        return id;
+    }
+    const int dnode = morton_prefix(k, l, u);
+    // last m in [l, u-1] with prefix(l, m) > dnode (prefix(l, .) does not grow along the keys)
+    int a = l, b = u - 1;
+    while (a < b) {
+        const int m = (a + b + 1) / 2;
+        if (morton_prefix(k, l, m) > dnode) a = m;
+        else b = m - 1;
+    }
+    const int m = a;
+    // split axis of the first differing bit (1..3), 1 when only the positions differ
+    nd.dnum = dnode < 64 ? 1 + (2 - (63 - dnode) % 3) : 1;
+    tp.nodes[id] = nd;
+    int left = build_morton_range(tp, k, l, m, bucket);
+    int right = build_morton_range(tp, k, m + 1, u, bucket);
+    tp.nodes[id].left = left;
+    tp.nodes[id].right = right;
+    return id;
+}
+
+static void morton_sums(Tree &tp, int np, double *s) {
+    Node &nd = tp.nodes[np];
+    if (nd.dnum == 0) {
+        s[0] = s[1] = s[2] = 0.0;
+        for (int i = nd.l; i <= nd.u; ++i)
+            for (int c = 0; c < 3; ++c) s[c] += tp.theData[3 * tp.indexes[i] + c];
+    } else {
+        double sl[3], sr[3];
+        morton_sums(tp, nd.left, sl);
+        morton_sums(tp, nd.right, sr);
+        for (int c = 0; c < 3; ++c) s[c] = sl[c] + sr[c];
+    }
+    Node &me = tp.nodes[np];
+    double radius = 0;
+    for (int c = 0; c < 3; ++c) me.X[c] = s[c] / me.n;
+    for (int i = me.l; i <= me.u; ++i) {
+        double dx[3];
+        for (int c = 0; c < 3; ++c) dx[c] = tp.theData[3 * tp.indexes[i] + c] - me.X[c];
+        double dist = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+        if (dist > radius) radius = dist;
+    }
+    me.oradius = 1.0 / radius;
 }
 
 static void label_nodes(Tree &tp, int np, int level) {
@@ -938,10 +1042,20 @@ static int create_tree(Ctx &c, const double *uniquePts, int nUnique, const int *
     tp.indexes.resize(nUnique);
     std::iota(tp.indexes.begin(), tp.indexes.end(), 0);
     tp.nodes.reserve(2 * nUnique);
-    tp.root = build_range(tp, 0, nUnique - 1, c.o.bucketSize);
-    tp.maxDepth = 1;
-    label_nodes(tp, tp.root, 1);
-    set_centers(tp, tp.root);
+    if (c.o.treeBuild == 1) {
+        std::vector<unsigned long long> codes;
+        morton_order(uniquePts, nUnique, codes, tp.indexes);
+        tp.root = build_morton_range(tp, codes, 0, nUnique - 1, c.o.bucketSize);
+        tp.maxDepth = 1;
+        label_nodes(tp, tp.root, 1);
+        double s[3];
+        morton_sums(tp, tp.root, s);
+    } else {
+        tp.root = build_range(tp, 0, nUnique - 1, c.o.bucketSize);
+        tp.maxDepth = 1;
+        label_nodes(tp, tp.root, 1);
+        set_centers(tp, tp.root);
+    }
     tp.Xu0.resize(3 * nUnique);
     for (int i = 0; i < nUnique; ++i)
         for (int k = 0; k < 3; ++k) tp.Xu0[3 * i + k] = uniquePts[3 * tp.indexes[i] + k];
@@ -1012,6 +1126,7 @@ static void unpack_opts(const double *v, Opts &o) {
     o.zeroCornerRotations = int(v[7]);
     o.cornerAngle = v[8];
     o.bucketSize = int(v[9]);
+    o.treeBuild = int(v[10]);
 }
 
 void orc_set_threads(int n) {

@@ -99,6 +99,7 @@ DEFAULT_OPTIONS = {
     "zeroCornerRotations": True,
     "cornerAngle": 30.0,
     "bucketSize": 8,
+    "treeBuild": "kd",
 }
 
 
@@ -112,6 +113,7 @@ def pack_options(opts):
             1.0 if o["useRotations"] else 0.0,
             1.0 if o["zeroCornerRotations"] else 0.0,
             o["cornerAngle"], float(o["bucketSize"]),
+            1.0 if o["treeBuild"] == "morton" else 0.0,
         ],
         dtype=np.float64,
     )
