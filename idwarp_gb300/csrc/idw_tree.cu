@@ -45,29 +45,19 @@ constexpr double kMortonCells = 2097152.0;  // 2^21
 constexpr unsigned kMortonMax = 2097151u;
 constexpr int kMaxTreeDepth = 128;
 
-template <class T>
-struct TreeBuf {
-    T *p = nullptr;
-    TreeBuf() = default;
-    TreeBuf(const TreeBuf &) = delete;
-    TreeBuf &operator=(const TreeBuf &) = delete;
-    ~TreeBuf() {
-        if (p) cudaFree(p);
-    }
-    bool alloc(size_t count) {
-        return cudaMalloc(reinterpret_cast<void **>(&p), std::max<size_t>(count, 1) * sizeof(T)) == cudaSuccess;
-    }
-};
-
 inline int grid_of(int64_t n, int b) { return int((n + b - 1) / b); }
 
-// Bounding box of the points (one block): box = (lo x, y, z, hi x, y, z).
-__global__ void k_tree_box(const double *pts, int n, double *box) {
+constexpr int kBoxBlocks = 64;  // partial bounding boxes
+constexpr int kRadChunk = 256;  // points per warp task of the radius pass
+
+// Partial bounding boxes: block b writes (lo x, y, z, hi x, y, z) of its
+// grid-stride share of the points to part[6 b ...].
+__global__ void k_tree_box(const double *pts, int n, double *part) {
     __shared__ double sLo[3][32], sHi[3][32];
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
         for (int c = 0; c < 3; ++c) {
-            const double x = pts[3 * int64_t(i) + c];
+            const double x = pts[3 * i + c];
             lo[c] = fmin(lo[c], x);
             hi[c] = fmax(hi[c], x);
         }
@@ -94,9 +84,25 @@ __global__ void k_tree_box(const double *pts, int n, double *box) {
         }
         if (lane == 0)
             for (int c = 0; c < 3; ++c) {
-                box[c] = lo[c];
-                box[3 + c] = hi[c];
+                part[6 * blockIdx.x + c] = lo[c];
+                part[6 * blockIdx.x + 3 + c] = hi[c];
             }
+    }
+}
+
+// The box of the partial boxes (one warp; minimum and maximum are exact in
+// any order).
+__global__ void k_tree_box_final(const double *part, int nPart, double *box) {
+    const int lane = threadIdx.x;
+    for (int c = 0; c < 6; ++c) {
+        const bool isLo = c < 3;
+        double v = isLo ? INFINITY : -INFINITY;
+        for (int b = lane; b < nPart; b += 32) v = isLo ? fmin(v, part[6 * b + c]) : fmax(v, part[6 * b + c]);
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = isLo ? fmin(v, w) : fmax(v, w);
+        }
+        if (lane == 0) box[c] = v;
     }
 }
 
@@ -183,11 +189,17 @@ __global__ void k_tree_keep(const int2 *range, const int *parent, int n, int buc
     if (keep) atomicAdd(count, 1u);
 }
 
-// Kept node k (preorder): range, escape, leaf flag, depth; pre[radix id] = k.
-__global__ void k_tree_nodes(const unsigned long long *key, const int *rid, int nn, int bucket, const int *parent,
-                             int4 *info, int *depth, int *pre) {
+// Kept node k (preorder): range, escape, leaf flag, depth; pre[radix id] = k;
+// chunks[k] = radius-pass tasks of the node (0 past the nn kept nodes).
+__global__ void k_tree_nodes(const unsigned long long *key, const int *rid, const unsigned *count, int nr,
+                             int bucket, const int *parent, int4 *info, int *depth, int *pre, int *chunks) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= nr) return;
+    const int nn = int(*count);
+    if (k >= nn) {
+        chunks[k] = 0;
+        return;
+    }
     const unsigned long long kk = key[k];
     const int l = int(kk >> 32), u = int(0xffffffffu - unsigned(kk & 0xffffffffull));
     const unsigned long long target = (unsigned long long)unsigned(u + 1) << 32;
@@ -202,6 +214,7 @@ __global__ void k_tree_nodes(const unsigned long long *key, const int *rid, int 
     for (int p = parent[rid[k]]; p >= 0 && dep < kMaxTreeDepth; p = parent[p]) ++dep;
     depth[k] = dep;
     pre[rid[k]] = k;
+    chunks[k] = (u - l + kRadChunk) / kRadChunk;
 }
 
 // Tree-order points: tp[i] = pts[perm[i]].
@@ -215,10 +228,11 @@ __global__ void k_tree_gather(const double *pts, const int *perm, int n, double 
 // Centroid sums bottom-up: each leaf sums its points in order, then climbs;
 // at each interior node the second child to arrive forms left + right (always
 // in that order) and goes on.  X = sum / count.
-__global__ void k_tree_sums(const int4 *info, const int *rid, const int *parent, const int *pre, int nn,
-                            const double *tp, double *sum, unsigned *arrived, double *X) {
+__global__ void k_tree_sums(const int4 *info, const int *rid, const int *parent, const int *pre,
+                            const unsigned *count, int nr, const double *tp, double *sum, unsigned *arrived,
+                            double *X) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nn) return;
+    if (k >= nr || k >= int(*count)) return;
     const int4 g = info[k];
     if (!g.w) return;
     double s[3] = {0.0, 0.0, 0.0};
@@ -245,23 +259,54 @@ __global__ void k_tree_sums(const int4 *info, const int *rid, const int *parent,
     }
 }
 
-// 1/max |x - X| over each node's points, one warp per node.
-__global__ void k_tree_radius(const int4 *info, int nn, const double *tp, const double *X, double *oradius) {
-    const int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+// Largest |x - X| over each node's points: one warp per task of up to
+// kRadChunk points of one node (tasks numbered through the inclusive sums of
+// the chunk counts), folded into the node's maximum with an integer atomic
+// on the bits (non-negative doubles order as their bit patterns).
+__global__ void k_tree_radius(const int4 *info, const unsigned *count, const int *incl, int nr, const double *tp,
+                              const double *X, unsigned long long *radBits) {
+    const int nn = int(*count);
+    const int total = incl[nr - 1];
     const int lane = threadIdx.x & 31;
-    if (w >= nn) return;
-    const int4 g = info[w];
-    const double cx = X[3 * w], cy = X[3 * w + 1], cz = X[3 * w + 2];
-    double r = 0.0;
-    for (int i = g.x + lane; i <= g.y; i += 32) {
-        const double dx = __dsub_rn(tp[3 * int64_t(i)], cx), dy = __dsub_rn(tp[3 * int64_t(i) + 1], cy),
-                     dz = __dsub_rn(tp[3 * int64_t(i) + 2], cz);
-        const double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
-        r = fmax(r, d);
+    const int nw = int((int64_t(gridDim.x) * blockDim.x) >> 5);
+    for (int c = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5); c < total; c += nw) {
+        int a = 0, b = nn - 1;  // first node k with incl[k] > c
+        while (a < b) {
+            const int m = (a + b) >> 1;
+            if (incl[m] > c) b = m;
+            else a = m + 1;
+        }
+        const int4 g = info[a];
+        const int first = incl[a] - (g.y - g.x + kRadChunk) / kRadChunk;
+        const int i0 = g.x + (c - first) * kRadChunk, i1 = min(g.y, i0 + kRadChunk - 1);
+        const double cx = X[3 * int64_t(a)], cy = X[3 * int64_t(a) + 1], cz = X[3 * int64_t(a) + 2];
+        double r = 0.0;
+        for (int i = i0 + lane; i <= i1; i += 32) {
+            const double dx = __dsub_rn(tp[3 * int64_t(i)], cx), dy = __dsub_rn(tp[3 * int64_t(i) + 1], cy),
+                         dz = __dsub_rn(tp[3 * int64_t(i) + 2], cz);
+            r = fmax(r, __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz))));
+        }
+        for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+        if (lane == 0) atomicMax(&radBits[a], (unsigned long long)__double_as_longlong(r));
     }
-    for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
-    if (lane == 0) oradius[w] = 1.0 / r;
 }
+
+__global__ void k_tree_oradius(const unsigned long long *radBits, const unsigned *count, int nr, double *oradius) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nr || k >= int(*count)) return;
+    oradius[k] = 1.0 / __longlong_as_double((long long)radBits[k]);
+}
+
+// Sub-buffers of one device allocation, each 256-byte aligned.
+struct Arena {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count) {
+        const size_t at = off;
+        off += (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
+        return at;
+    }
+};
 
 }  // namespace
 
@@ -271,72 +316,103 @@ int build_morton_tree(const double *pts, int n, int bucket, FlatTree &t, cudaStr
     t.bucket = bucket;
     if (n <= 0) return 0;
     if (n > (INT_MAX - 1) / 2) return -1;
-    const int nr = 2 * n - 1;  // radix nodes
-    TreeBuf<double> dPts, dBox, dTp, dSum, dX, dOr;
-    TreeBuf<unsigned long long> dCodes, dCodesS, dKey, dKeyS;
-    TreeBuf<int> dIdx, dPerm, dParent, dRid, dRidS, dPre, dDepth;
-    TreeBuf<int2> dRange;
-    TreeBuf<int4> dInfo;
-    TreeBuf<unsigned> dCount, dArrived;
-    TreeBuf<char> dTmp;
-    if (!dPts.alloc(3 * size_t(n)) || !dBox.alloc(6) || !dTp.alloc(3 * size_t(n)) || !dCodes.alloc(n) ||
-        !dCodesS.alloc(n) || !dIdx.alloc(n) || !dPerm.alloc(n) || !dParent.alloc(nr) || !dRange.alloc(n - 1) ||
-        !dKey.alloc(nr) || !dKeyS.alloc(nr) || !dRid.alloc(nr) || !dRidS.alloc(nr) || !dPre.alloc(nr) ||
-        !dCount.alloc(1))
-        return -2;
-    // cub scratch: the larger of the two sorts
-    size_t tmpA = 0, tmpB = 0;
-    if (cub::DeviceRadixSort::SortPairs(nullptr, tmpA, dCodes.p, dCodesS.p, dIdx.p, dPerm.p, n, 0, 63, st) !=
-            cudaSuccess ||
-        cub::DeviceRadixSort::SortPairs(nullptr, tmpB, dKey.p, dKeyS.p, dRid.p, dRidS.p, nr, 0, 64, st) !=
-            cudaSuccess)
+    const int nr = 2 * n - 1;  // radix nodes; at most nr are kept
+    // cub scratch: the larger of the two sorts and the scan
+    size_t tmpA = 0, tmpB = 0, tmpC = 0;
+    if (cub::DeviceRadixSort::SortPairs(nullptr, tmpA, (unsigned long long *)nullptr, (unsigned long long *)nullptr,
+                                        (int *)nullptr, (int *)nullptr, n, 0, 63, st) != cudaSuccess ||
+        cub::DeviceRadixSort::SortPairs(nullptr, tmpB, (unsigned long long *)nullptr, (unsigned long long *)nullptr,
+                                        (int *)nullptr, (int *)nullptr, nr, 0, 64, st) != cudaSuccess ||
+        cub::DeviceScan::InclusiveSum(nullptr, tmpC, (int *)nullptr, (int *)nullptr, nr, st) != cudaSuccess)
         return -1;
-    size_t tmp = std::max(tmpA, tmpB);
-    if (!dTmp.alloc(tmp)) return -2;
-    if (cudaMemcpyAsync(dPts.p, pts, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemsetAsync(dParent.p, 0xff, sizeof(int) * nr, st) != cudaSuccess ||
-        cudaMemsetAsync(dCount.p, 0, sizeof(unsigned), st) != cudaSuccess)
-        return -1;
-    k_tree_box<<<1, 1024, 0, st>>>(dPts.p, n, dBox.p);
-    k_tree_codes<<<grid_of(n, 256), 256, 0, st>>>(dPts.p, n, dBox.p, dCodes.p, dIdx.p);
-    if (cub::DeviceRadixSort::SortPairs(dTmp.p, tmp, dCodes.p, dCodesS.p, dIdx.p, dPerm.p, n, 0, 63, st) !=
-        cudaSuccess)
-        return -1;
-    if (n > 1) k_tree_radix<<<grid_of(n - 1, 256), 256, 0, st>>>(dCodesS.p, n, dRange.p, dParent.p);
-    k_tree_keep<<<grid_of(nr, 256), 256, 0, st>>>(dRange.p, dParent.p, n, bucket, dKey.p, dRid.p, dCount.p);
-    tmp = std::max(tmpA, tmpB);
-    if (cub::DeviceRadixSort::SortPairs(dTmp.p, tmp, dKey.p, dKeyS.p, dRid.p, dRidS.p, nr, 0, 64, st) !=
-        cudaSuccess)
-        return -1;
+    const size_t tmp = std::max(std::max(tmpA, tmpB), tmpC);
+    Arena ar;
+    const size_t oPts = ar.take<double>(3 * size_t(n)), oPart = ar.take<double>(6 * kBoxBlocks),
+                 oBox = ar.take<double>(6), oTp = ar.take<double>(3 * size_t(n)),
+                 oCodes = ar.take<unsigned long long>(n), oCodesS = ar.take<unsigned long long>(n),
+                 oIdx = ar.take<int>(n), oPerm = ar.take<int>(n), oParent = ar.take<int>(nr),
+                 oRange = ar.take<int2>(n - 1), oKey = ar.take<unsigned long long>(nr),
+                 oKeyS = ar.take<unsigned long long>(nr), oRid = ar.take<int>(nr), oRidS = ar.take<int>(nr),
+                 oPre = ar.take<int>(nr), oCount = ar.take<unsigned>(1), oInfo = ar.take<int4>(nr),
+                 oDepth = ar.take<int>(nr), oSum = ar.take<double>(3 * size_t(nr)), oX = ar.take<double>(3 * size_t(nr)),
+                 oOr = ar.take<double>(nr), oRad = ar.take<unsigned long long>(nr), oArr = ar.take<unsigned>(nr),
+                 oChunks = ar.take<int>(nr), oIncl = ar.take<int>(nr), oTmp = ar.take<char>(tmp);
+    char *base = nullptr;
+    if (cudaMalloc(&base, ar.off) != cudaSuccess) return -2;
+    auto at = [&](size_t o) { return static_cast<void *>(base + o); };
+    double *dPts = (double *)at(oPts), *dPart = (double *)at(oPart), *dBox = (double *)at(oBox),
+           *dTp = (double *)at(oTp), *dSum = (double *)at(oSum), *dX = (double *)at(oX), *dOr = (double *)at(oOr);
+    unsigned long long *dCodes = (unsigned long long *)at(oCodes), *dCodesS = (unsigned long long *)at(oCodesS),
+                       *dKey = (unsigned long long *)at(oKey), *dKeyS = (unsigned long long *)at(oKeyS),
+                       *dRad = (unsigned long long *)at(oRad);
+    int *dIdx = (int *)at(oIdx), *dPerm = (int *)at(oPerm), *dParent = (int *)at(oParent), *dRid = (int *)at(oRid),
+        *dRidS = (int *)at(oRidS), *dPre = (int *)at(oPre), *dDepth = (int *)at(oDepth), *dChunks = (int *)at(oChunks),
+        *dIncl = (int *)at(oIncl);
+    int2 *dRange = (int2 *)at(oRange);
+    int4 *dInfo = (int4 *)at(oInfo);
+    unsigned *dCount = (unsigned *)at(oCount), *dArr = (unsigned *)at(oArr);
+    void *dTmp = at(oTmp);
+    int sms = 0, dev = 0;
+    int rc = 0;
+    size_t tb = tmp;
+    const int boxBlocks = std::min(kBoxBlocks, grid_of(n, 1024));
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaMemcpyAsync(dPts, pts, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(dParent, 0xff, sizeof(int) * nr, st) != cudaSuccess ||
+        cudaMemsetAsync(dCount, 0, sizeof(unsigned), st) != cudaSuccess ||
+        cudaMemsetAsync(dArr, 0, sizeof(unsigned) * nr, st) != cudaSuccess ||
+        cudaMemsetAsync(dRad, 0, sizeof(unsigned long long) * nr, st) != cudaSuccess) {
+        rc = -1;
+    } else {
+        k_tree_box<<<boxBlocks, 1024, 0, st>>>(dPts, n, dPart);
+        k_tree_box_final<<<1, 32, 0, st>>>(dPart, boxBlocks, dBox);
+        k_tree_codes<<<grid_of(n, 256), 256, 0, st>>>(dPts, n, dBox, dCodes, dIdx);
+        if (cub::DeviceRadixSort::SortPairs(dTmp, tb, dCodes, dCodesS, dIdx, dPerm, n, 0, 63, st) != cudaSuccess)
+            rc = -1;
+    }
+    if (rc == 0) {
+        if (n > 1) k_tree_radix<<<grid_of(n - 1, 256), 256, 0, st>>>(dCodesS, n, dRange, dParent);
+        k_tree_keep<<<grid_of(nr, 256), 256, 0, st>>>(dRange, dParent, n, bucket, dKey, dRid, dCount);
+        tb = tmp;
+        if (cub::DeviceRadixSort::SortPairs(dTmp, tb, dKey, dKeyS, dRid, dRidS, nr, 0, 64, st) != cudaSuccess)
+            rc = -1;
+    }
+    if (rc == 0) {
+        k_tree_nodes<<<grid_of(nr, 256), 256, 0, st>>>(dKeyS, dRidS, dCount, nr, bucket, dParent, dInfo, dDepth, dPre,
+                                                       dChunks);
+        k_tree_gather<<<grid_of(n, 256), 256, 0, st>>>(dPts, dPerm, n, dTp);
+        k_tree_sums<<<grid_of(nr, 128), 128, 0, st>>>(dInfo, dRidS, dParent, dPre, dCount, nr, dTp, dSum, dArr, dX);
+        tb = tmp;
+        if (cub::DeviceScan::InclusiveSum(dTmp, tb, dChunks, dIncl, nr, st) != cudaSuccess) rc = -1;
+    }
+    if (rc == 0) {
+        k_tree_radius<<<8 * std::max(sms, 1), 256, 0, st>>>(dInfo, dCount, dIncl, nr, dTp, dX, dRad);
+        k_tree_oradius<<<grid_of(nr, 256), 256, 0, st>>>(dRad, dCount, nr, dOr);
+        if (cudaGetLastError() != cudaSuccess) rc = -1;
+    }
     unsigned nnU = 0;
-    if (cudaMemcpyAsync(&nnU, dCount.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-        return -1;
+    if (rc == 0 && (cudaMemcpyAsync(&nnU, dCount, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                    cudaStreamSynchronize(st) != cudaSuccess || nnU < 1 || nnU > unsigned(nr)))
+        rc = -1;
     const int nn = int(nnU);
-    if (nn < 1 || nn > nr) return -1;
-    if (!dInfo.alloc(nn) || !dDepth.alloc(nn) || !dSum.alloc(3 * size_t(nn)) || !dX.alloc(3 * size_t(nn)) ||
-        !dOr.alloc(nn) || !dArrived.alloc(nn))
-        return -2;
-    if (cudaMemsetAsync(dArrived.p, 0, sizeof(unsigned) * nn, st) != cudaSuccess) return -1;
-    k_tree_nodes<<<grid_of(nn, 256), 256, 0, st>>>(dKeyS.p, dRidS.p, nn, bucket, dParent.p, dInfo.p, dDepth.p,
-                                                   dPre.p);
-    k_tree_gather<<<grid_of(n, 256), 256, 0, st>>>(dPts.p, dPerm.p, n, dTp.p);
-    k_tree_sums<<<grid_of(nn, 128), 128, 0, st>>>(dInfo.p, dRidS.p, dParent.p, dPre.p, nn, dTp.p, dSum.p,
-                                                  dArrived.p, dX.p);
-    k_tree_radius<<<grid_of(32 * int64_t(nn), 256), 256, 0, st>>>(dInfo.p, nn, dTp.p, dX.p, dOr.p);
-    if (cudaGetLastError() != cudaSuccess) return -1;
-    std::vector<int4> info(nn);
-    t.perm.resize(n);
-    t.depth.resize(nn);
-    t.X.resize(3 * size_t(nn));
-    t.oradius.resize(nn);
-    if (cudaMemcpyAsync(t.perm.data(), dPerm.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(info.data(), dInfo.p, sizeof(int4) * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(t.depth.data(), dDepth.p, sizeof(int) * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(t.X.data(), dX.p, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(t.oradius.data(), dOr.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-        return -1;
+    std::vector<int4> info;
+    if (rc == 0) {
+        info.resize(nn);
+        t.perm.resize(n);
+        t.depth.resize(nn);
+        t.X.resize(3 * size_t(nn));
+        t.oradius.resize(nn);
+        if (cudaMemcpyAsync(t.perm.data(), dPerm, sizeof(int) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(info.data(), dInfo, sizeof(int4) * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(t.depth.data(), dDepth, sizeof(int) * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(t.X.data(), dX, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(t.oradius.data(), dOr, sizeof(double) * nn, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            rc = -1;
+    }
+    cudaFree(base);
+    if (rc != 0) return rc;
     t.l.resize(nn);
     t.u.resize(nn);
     t.escape.resize(nn);
