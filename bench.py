@@ -666,13 +666,24 @@ def run_case(case, cfg, reps):
     """One operation on a config's mesh, repeated: the small cases the ncu
     captures profile (warp: warpMesh; deriv1: warpDeriv of one seed, double-float
     form; deriv1fast: the FP32 form; deriv16 / deriv16fast: 16 seeds in one
-    call; batch: 8 surfaces through warpMeshBatch)."""
+    call; batch: 8 surfaces through warpMeshBatch; setup: the surface
+    definition, tree included, with the tree of --tree-build)."""
     import torch
 
     from idwarp_gb300 import _lib
     from idwarp_gb300 import synthetic as S
 
     m = make_workload(cfg)
+    if case == "setup":
+        out = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            mesh = build_mesh(m, "mixed")
+            torch.cuda.synchronize()
+            out.append({"setup_s": time.perf_counter() - t0, "treeBuildMs": mesh.getStats()["treeBuildMs"]})
+            del mesh
+        print(json.dumps({"case": case, "config": cfg, "reps": reps, "tree": TREE_BUILD, "runs": out}))
+        return 0
     mesh = build_mesh(m, "mixed")
     L = mesh.lib
     L.idw_set_stream(mesh.ctx, C.c_void_p(torch.cuda.current_stream().cuda_stream))
@@ -730,7 +741,7 @@ def main():
                     help="surface tree: the reference's kd tree (host) or the Morton tree (GPU)")
     ap.add_argument("--walk-lists", default="auto", choices=["auto", "off"],
                     help="mixed fast mode: replay recorded walk decisions (auto) or decide in every walk (off)")
-    ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "deriv16", "deriv16fast", "batch"],
+    ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "deriv16", "deriv16fast", "batch", "setup"],
                     help="run one operation --steps times on --config's mesh (the small profiling cases)")
     args = ap.parse_args()
     global WALK_LISTS, TREE_BUILD

@@ -105,6 +105,7 @@ class USMesh(BaseSolver):
             "adjointPrecision": [str, ["precise", "fast"]],
             "walkLists": [str, ["auto", "off"]],
             "treeBuild": [str, ["kd", "morton"]],
+            "deterministic": [bool, False],
         }
 
     # ------------------------------------------------------------------
@@ -566,6 +567,7 @@ class USMesh(BaseSolver):
         o.adjointPrecision = {"precise": _lib.IDW_ADJ_PRECISE, "fast": _lib.IDW_ADJ_FAST}[self.getOption("adjointPrecision")]
         o.walkLists = {"auto": _lib.IDW_WALK_LISTS_AUTO, "off": _lib.IDW_WALK_LISTS_OFF}[self.getOption("walkLists")]
         o.treeBuild = {"kd": _lib.IDW_TREE_KD, "morton": _lib.IDW_TREE_MORTON}[self.getOption("treeBuild")]
+        o.deterministic = int(self.getOption("deterministic"))
 
     def _setMeshOptions(self):
         """Push the current options to the library (idwarp/UnstructuredMesh.py:1051-1069)."""

@@ -44,7 +44,8 @@ class idw_options(C.Structure):
         ("evalMode", C.c_int32), ("useRotations", C.c_int32), ("zeroCornerRotations", C.c_int32),
         ("bucketSize", C.c_int32), ("precision", C.c_int32), ("diagnostics", C.c_int32),
         ("mixedGate", C.c_double), ("exactSchedule", C.c_int32), ("adjointPrecision", C.c_int32),
-        ("walkLists", C.c_int32), ("treeBuild", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("walkLists", C.c_int32), ("treeBuild", C.c_int32), ("deterministic", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 

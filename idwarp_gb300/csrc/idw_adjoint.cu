@@ -35,20 +35,21 @@ struct AdjSmem {
 
 // Lands the four moment sums of term `target`, seed component c (seed s, axis
 // a): w -> B (slot 9 + a), w (r - C) -> row a of P (slots 3a .. 3a + 2).
+template <bool DET>
 __device__ __forceinline__ void land_moments(double *adj, int64_t seedStride, int c, int64_t target, float w,
                                              float m0, float m1, float m2) {
     if (w == 0.f && m0 == 0.f && m1 == 0.f && m2 == 0.f) return;
     const int s = c / 3, a = c - 3 * s;
     double *d = adj + s * seedStride + 12 * target;
-    atomicAdd(d + 9 + a, double(w));
-    atomicAdd(d + 3 * a + 0, double(m0));
-    atomicAdd(d + 3 * a + 1, double(m1));
-    atomicAdd(d + 3 * a + 2, double(m2));
+    land_add<DET>(d + 9 + a, double(w));
+    land_add<DET>(d + 3 * a + 0, double(m0));
+    land_add<DET>(d + 3 * a + 1, double(m1));
+    land_add<DET>(d + 3 * a + 2, double(m2));
 }
 
 // Warp reduction of m point contributions (vb[0..m)) against the lanes'
 // seeds, blocked for many seeds: lane c owns seed component c and all m terms.
-template <int S>
+template <int S, bool DET>
 __device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *targets, double *adj,
                                              int64_t seedStride) {
     constexpr int kChunk = AdjSmem<S>::kChunk;
@@ -76,10 +77,10 @@ __device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *t
         for (int p = 0; p < kChunk; ++p) {
             if (p < m && (acc[p][0] != 0.f || acc[p][1] != 0.f || acc[p][2] != 0.f || acc[p][3] != 0.f)) {
                 double *d = adj + s * seedStride + 12 * int64_t(targets[p]);
-                atomicAdd(d + 9 + a, double(acc[p][0]));
-                atomicAdd(d + 3 * a + 0, double(acc[p][1]));
-                atomicAdd(d + 3 * a + 1, double(acc[p][2]));
-                atomicAdd(d + 3 * a + 2, double(acc[p][3]));
+                land_add<DET>(d + 9 + a, double(acc[p][0]));
+                land_add<DET>(d + 3 * a + 0, double(acc[p][1]));
+                land_add<DET>(d + 3 * a + 1, double(acc[p][2]));
+                land_add<DET>(d + 3 * a + 2, double(acc[p][3]));
             }
         }
     }
@@ -90,7 +91,7 @@ __device__ __forceinline__ void reduce_terms(AdjSmem<S> &sm, int m, const int *t
 // every (32/S)-th point of the chunk, lane s = lane % S all three axes of seed
 // s, so all 32 lanes work where the blocked form keeps 24 (13% faster at 8M
 // nodes; for 16 seeds the blocked form measured faster and stays).
-template <int S>
+template <int S, bool DET>
 __device__ __forceinline__ void reduce_groups(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
     constexpr int G = 32 / S;
     constexpr int P = (AdjSmem<S>::kChunk + G - 1) / G;
@@ -123,7 +124,7 @@ __device__ __forceinline__ void reduce_groups(AdjSmem<S> &sm, int m, int base, d
         if (g + G * q < m)
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                land_moments(adj, seedStride, 3 * s + a, base + g + G * q, acc[q][a][0], acc[q][a][1], acc[q][a][2],
+                land_moments<DET>(adj, seedStride, 3 * s + a, base + g + G * q, acc[q][a][0], acc[q][a][1], acc[q][a][2],
                              acc[q][a][3]);
     __syncwarp();
 }
@@ -132,7 +133,7 @@ __device__ __forceinline__ void reduce_groups(AdjSmem<S> &sm, int m, int base, d
 // task, so that 3 S m tasks keep the warp busy where 3 S lanes alone would
 // not.  Each task walks the lanes starting at its term index, which spreads
 // the tasks of different terms over the shared-memory banks.
-template <int S>
+template <int S, bool DET>
 __device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
@@ -149,13 +150,14 @@ __device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, do
             a2 = fmaf(v.z, nbv, a2);
             a3 = fmaf(v.w, nbv, a3);
         }
-        land_moments(adj, seedStride, c, base + p, a0, a1, a2, a3);
+        land_moments<DET>(adj, seedStride, c, base + p, a0, a1, a2, a3);
     }
     __syncwarp();
 }
 
 // One seed, one term: the 12 products v (x) n of every lane summed over the
 // warp (warp_land_moments).  Called by all 32 lanes.
+template <bool DET>
 __device__ __forceinline__ void reduce_one_s1(const float4 v, const float n[3], double *d) {
     const float vc[4] = {v.x, v.y, v.z, v.w};
     float P[12];
@@ -163,11 +165,12 @@ __device__ __forceinline__ void reduce_one_s1(const float4 v, const float n[3], 
     for (int k = 0; k < 4; ++k)
 #pragma unroll
         for (int a = 0; a < 3; ++a) P[3 * k + a] = vc[k] * n[a];
-    warp_land_moments(P, d);
+    warp_land_moments<DET>(P, d);
 }
 
 // REPLAY: walk the recorded decisions (idw_replay.cu) instead of deciding.
-template <int S, int KIND, int REPLAY>
+// DET: order-independent landings (idw_land.cuh).
+template <int S, int KIND, int REPLAY, bool DET = false>
 __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, PointsDevF pf, VolumeDev v,
                                                        WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
                                                        const double *dxv, int64_t dxvStride, const double *den,
@@ -272,11 +275,11 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                             sm.vb[p][lane] = make_float4(w, w * R0, w * R1, w * R2);
                         }
                         if constexpr (S <= 4)
-                            reduce_tasks<S>(sm, m, i0, ptAdj, ptStride);
+                            reduce_tasks<S, DET>(sm, m, i0, ptAdj, ptStride);
                         else if constexpr (S == 8)
-                            reduce_groups<S>(sm, m, i0, ptAdj, ptStride);
+                            reduce_groups<S, DET>(sm, m, i0, ptAdj, ptStride);
                         else
-                            reduce_terms<S>(sm, m, targets, ptAdj, ptStride);
+                            reduce_terms<S, DET>(sm, m, targets, ptAdj, ptStride);
                     }
                 }
                 if (!REPLAY) node = inf.z;
@@ -306,14 +309,14 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                     }
                     const float4 vv = make_float4(w, w * rho0, w * rho1, w * rho2);
                     if constexpr (S == 1) {
-                        reduce_one_s1(vv, nl, nodeAdj + 12 * int64_t(node));
+                        reduce_one_s1<DET>(vv, nl, nodeAdj + 12 * int64_t(node));
                     } else {
                         sm.vb[0][lane] = vv;
                         if constexpr (S <= 4) {
-                            reduce_tasks<S>(sm, 1, node, nodeAdj, nodeStride);
+                            reduce_tasks<S, DET>(sm, 1, node, nodeAdj, nodeStride);
                         } else {
                             targets[0] = node;
-                            reduce_terms<S>(sm, 1, targets, nodeAdj, nodeStride);
+                            reduce_terms<S, DET>(sm, 1, targets, nodeAdj, nodeStride);
                         }
                     }
                 }
@@ -376,10 +379,15 @@ template <int S, int KIND>
 void launch_adj(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
                 const MixedParams &mp, const Law32<KIND> &law, int exact, const double *dxv, int64_t dxvStride,
                 const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj, int64_t nodeStride,
-                unsigned long long *counters, const WalkLists &wl, cudaStream_t st) {
+                unsigned long long *counters, const WalkLists &wl, cudaStream_t st, int det) {
     const size_t smem = 4 * sizeof(AdjSmem<S>);
     const int g = int((v.nVol + 127) / 128);
-    if (wl.list && !exact) {
+    if (det) {  // order-independent landings: the deciding walk
+        cudaFuncSetAttribute(k_adjoint_mixed<S, KIND, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem));
+        k_adjoint_mixed<S, KIND, 0, true><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride,
+                                                                den, ptAdj, ptStride, nodeAdj, nodeStride, counters, wl);
+    } else if (wl.list && !exact) {
         launch_add_walk_counters(counters, wl.counters, st);
         cudaFuncSetAttribute(k_adjoint_mixed<S, KIND, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         k_adjoint_mixed<S, KIND, 1><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv, dxvStride, den,
@@ -395,16 +403,17 @@ template <int S>
 void launch_adj_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                     const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, int exact, const double *dxv,
                     int64_t dxvStride, const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj,
-                    int64_t nodeStride, unsigned long long *counters, const WalkLists &lists, cudaStream_t st) {
+                    int64_t nodeStride, unsigned long long *counters, const WalkLists &lists, cudaStream_t st,
+                    int det) {
     if (wl.isInt && wl.ia == 3 && wl.ib == 5) {
         launch_adj<S, 0>(t, tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, dxv, dxvStride, den, ptAdj, ptStride,
-                         nodeAdj, nodeStride, counters, lists, st);
+                         nodeAdj, nodeStride, counters, lists, st, det);
     } else if (wl.isInt) {
         launch_adj<S, 1>(t, tf, pf, v, rec, mp, Law32<1>{wl.ia, wl.ib, float(wl.aExp), float(wl.bExp)}, exact, dxv,
-                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, lists, st);
+                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, lists, st, det);
     } else {
         launch_adj<S, 2>(t, tf, pf, v, rec, mp, Law32<2>{0, 0, float(wl.aExp), float(wl.bExp)}, exact, dxv,
-                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, lists, st);
+                         dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, counters, lists, st, det);
     }
 }
 
@@ -421,7 +430,8 @@ void launch_adjoint_combine(const TreeDev &t, const dbl4 *ptXA, int nPts, int nS
 int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
-                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st, int maxGroup) {
+                         const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st, int maxGroup,
+                         int combine, int det) {
     if (nSeeds <= 0) return 0;
     const MixedParams mp = make_mixed_params(k);
     const int64_t ptStride = 12 * int64_t(nPts), nodeStride = 12 * int64_t(t.nNodes);
@@ -440,29 +450,32 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
         // seeds in groups of 16, 8, 4 or 1 sharing one walk, none above maxGroup
         if (left >= 16 && maxGroup >= 16) {
             launch_adj_law<16>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                               counters, k.lists, st);
+                               counters, k.lists, st, det);
             s0 += 16;
         } else if (left >= 8 && maxGroup >= 8) {
             launch_adj_law<8>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                              counters, k.lists, st);
+                              counters, k.lists, st, det);
             s0 += 8;
         } else if (left >= 4 && maxGroup >= 4) {
             launch_adj_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                              counters, k.lists, st);
+                              counters, k.lists, st, det);
             s0 += 4;
         } else if (tiledOne) {
-            launch_exact_adjoint(tf, pf, v, rec, mp, k.law, d, den, pa, counters, st);
+            launch_exact_adjoint(tf, pf, v, rec, mp, k.law, d, den, pa, counters, st, det);
             s0 += 1;
         } else {
             launch_adj_law<1>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                              counters, k.lists, st);
+                              counters, k.lists, st, det);
             s0 += 1;
         }
     }
+    if (!combine) return 0;
     const int64_t total = int64_t(nPts) * nSeeds;
     k_adjoint_combine<<<int((total + 127) / 128), 128, 0, st>>>(t, ptXA, nPts, nSeeds, ptAcc, ptStride, nodeAcc,
                                                                 nodeStride, ptAdj);
     return 0;
 }
+
+IDW_LAND_SETTER(land_set_adjoint)
 
 }  // namespace idw

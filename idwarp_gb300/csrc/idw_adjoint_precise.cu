@@ -55,14 +55,15 @@ __device__ __forceinline__ void df_fma_acc(dfl &acc, dfl a, dfl b) {
     acc.h = s;
 }
 
+template <bool DET>
 __device__ __forceinline__ void land_df(double *d, dfl v) {
-    if (v.h != 0.f || v.l != 0.f) atomicAdd(d, double(v.h) + double(v.l));
+    if (v.h != 0.f || v.l != 0.f) land_add<DET>(d, double(v.h) + double(v.l));
 }
 
 // Reduction of m terms (vh/vl[0..m)) against the lanes' seeds: one (term,
 // seed component) pair per lane task, each summing the 32 lanes in
 // double-float; lands w -> slot 9 + a and w (r - C) -> slots 3 a .. 3 a + 2.
-template <int S>
+template <int S, bool DET>
 __device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
@@ -80,10 +81,10 @@ __device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base
         }
         const int s = c / 3, a = c - 3 * s;
         double *d = adj + s * seedStride + 12 * int64_t(base + p);
-        land_df(d + 9 + a, a0);
-        land_df(d + 3 * a + 0, a1);
-        land_df(d + 3 * a + 1, a2);
-        land_df(d + 3 * a + 2, a3);
+        land_df<DET>(d + 9 + a, a0);
+        land_df<DET>(d + 3 * a + 0, a1);
+        land_df<DET>(d + 3 * a + 1, a2);
+        land_df<DET>(d + 3 * a + 2, a3);
     }
     __syncwarp();
 }
@@ -91,6 +92,7 @@ __device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base
 // One seed, one term: the 12 products v (x) n summed over the warp in
 // double-float (two halving exchanges, then three butterflies, as
 // warp_land_moments), landed by lanes 0..2 of each lane group.
+template <bool DET>
 __device__ __forceinline__ void land_one_df(const dfl v[4], const dfl n[3], double *d) {
     const int lane = threadIdx.x & 31;
     dfl P[12];
@@ -126,7 +128,7 @@ __device__ __forceinline__ void land_one_df(const dfl v[4], const dfl n[3], doub
             R[k] = df_add(R[k], got);
         }
     const int G = lane >> 3, a = lane & 7;
-    if (a < 3) land_df(d + (G == 0 ? 9 + a : 3 * a + G - 1), a == 0 ? R[0] : (a == 1 ? R[1] : R[2]));
+    if (a < 3) land_df<DET>(d + (G == 0 ? 9 + a : 3 * a + G - 1), a == 0 ? R[0] : (a == 1 ? R[1] : R[2]));
 }
 
 // (r - C) of a lane as a double-float per axis: exact high-part differences
@@ -153,7 +155,8 @@ __device__ __forceinline__ void term_vector(float wh, float wl, const dfl x[3], 
 // S > 0: S seeds (dxv, common order, stride dxvStride) into ptAdj / nodeAdj.
 // S = 0: the denominator walk; denOut receives sum w in true units (common order).
 // REPLAY: walk the recorded decisions (idw_replay.cu) instead of deciding.
-template <int S, int KIND, int REPLAY>
+// DET: order-independent landings (idw_land.cuh).
+template <int S, int KIND, int REPLAY, bool DET = false>
 __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf, PointsDevF pf, VolumeDev v,
                                                          WalkRecF rec, MixedParams mp, Law32<KIND> law, int exact,
                                                          const double *dxv, int64_t dxvStride, const double *den,
@@ -260,7 +263,7 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                             sm.vl[p][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
                         }
                     }
-                    if constexpr (S > 0) reduce_tasks_df<S>(sm, m, i0, ptAdj, ptStride);
+                    if constexpr (S > 0) reduce_tasks_df<S, DET>(sm, m, i0, ptAdj, ptStride);
                 }
                 if (!REPLAY) node = inf.z;
             } else {
@@ -294,11 +297,11 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                         dfl vv[4];
                         term_vector(wh, wl, x, vv);
                         if constexpr (S == 1) {
-                            land_one_df(vv, nl1, nodeAdj + 12 * int64_t(node));
+                            land_one_df<DET>(vv, nl1, nodeAdj + 12 * int64_t(node));
                         } else {
                             sm.vh[0][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
                             sm.vl[0][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
-                            reduce_tasks_df<S>(sm, 1, node, nodeAdj, nodeStride);
+                            reduce_tasks_df<S, DET>(sm, 1, node, nodeAdj, nodeStride);
                         }
                     }
                 }
@@ -318,9 +321,19 @@ template <int S, int KIND>
 void launch_prec(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
                  const MixedParams &mp, const Law32<KIND> &law, int exact, const double *dxv, int64_t dxvStride,
                  const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj, int64_t nodeStride,
-                 double *denOut, unsigned long long *counters, const WalkLists &wl, cudaStream_t st) {
+                 double *denOut, unsigned long long *counters, const WalkLists &wl, cudaStream_t st, int det) {
     const size_t smem = 4 * sizeof(PrecSmem<S>);
     const int g = int((v.nVol + 127) / 128);
+    if constexpr (S > 0) {
+        if (det) {  // order-independent landings: the deciding walk
+            cudaFuncSetAttribute(k_adjoint_precise<S, KIND, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem));
+            k_adjoint_precise<S, KIND, 0, true><<<g, 128, smem, st>>>(t, tf, pf, v, rec, mp, law, exact, dxv,
+                                                                      dxvStride, den, ptAdj, ptStride, nodeAdj,
+                                                                      nodeStride, denOut, counters, wl);
+            return;
+        }
+    }
     // sixteen seeds keep deciding as they go: at four blocks per SM (shared
     // memory) the replay's schedule measured slower (8M-node wing: 622 against
     // 586 ms with 4 points per pass); fewer seeds replay (one seed 73 against
@@ -344,13 +357,13 @@ void launch_prec_law(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf,
                      const WalkRecF &rec, const MixedParams &mp, const WeightLaw &wl, int exact, const double *dxv,
                      int64_t dxvStride, const double *den, double *ptAdj, int64_t ptStride, double *nodeAdj,
                      int64_t nodeStride, double *denOut, unsigned long long *counters, const WalkLists &lists,
-                     cudaStream_t st) {
+                     cudaStream_t st, int det) {
     if (wl.isInt && wl.ia == 3 && wl.ib == 5)
         launch_prec<S, 0>(t, tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, exact, dxv, dxvStride, den, ptAdj,
-                          ptStride, nodeAdj, nodeStride, denOut, counters, lists, st);
+                          ptStride, nodeAdj, nodeStride, denOut, counters, lists, st, det);
     else
         launch_prec<S, 1>(t, tf, pf, v, rec, mp, Law32<1>{wl.ia, wl.ib, float(wl.aExp), float(wl.bExp)}, exact, dxv,
-                          dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, denOut, counters, lists, st);
+                          dxvStride, den, ptAdj, ptStride, nodeAdj, nodeStride, denOut, counters, lists, st, det);
 }
 
 }  // namespace
@@ -363,13 +376,13 @@ void launch_precise_denominator(const TreeDev &t, const TreeDevF &tf, const Poin
     if (v.nVol <= 0) return;
     const MixedParams mp = make_mixed_params(k);
     launch_prec_law<0>(t, tf, pf, v, rec, mp, k.law, exact, nullptr, 0, nullptr, nullptr, 0, nullptr, 0, denOut,
-                       nullptr, k.lists, st);
+                       nullptr, k.lists, st, 0);
 }
 
 int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                            const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                            int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, int nPts,
-                           unsigned long long *counters, cudaStream_t st) {
+                           unsigned long long *counters, cudaStream_t st, int det) {
     if (nSeeds <= 0 || v.nVol <= 0) return 0;
     const MixedParams mp = make_mixed_params(k);
     const int64_t ptStride = 12 * int64_t(nPts), nodeStride = 12 * int64_t(t.nNodes);
@@ -380,19 +393,21 @@ int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDev
         double *pa = ptAcc + s0 * ptStride, *na = nodeAcc + s0 * nodeStride;
         if (left >= 16) {
             launch_prec_law<16>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                                nullptr, counters, k.lists, st);
+                                nullptr, counters, k.lists, st, det);
             s0 += 16;
         } else if (left >= 4) {
             launch_prec_law<4>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                               nullptr, counters, k.lists, st);
+                               nullptr, counters, k.lists, st, det);
             s0 += 4;
         } else {
             launch_prec_law<1>(t, tf, pf, v, rec, mp, k.law, exact, d, dxvStride, den, pa, ptStride, na, nodeStride,
-                               nullptr, counters, k.lists, st);
+                               nullptr, counters, k.lists, st, det);
             s0 += 1;
         }
     }
     return 0;
 }
+
+IDW_LAND_SETTER(land_set_precise)
 
 }  // namespace idw

@@ -16,6 +16,7 @@
 #include "idw_host.hpp"
 #include "idw_cplx.cuh"
 #include "idw_kernels.h"
+#include "idw_land.cuh"
 
 using namespace idw;
 
@@ -91,6 +92,10 @@ struct Ctx {
     // warpDeriv accumulators (grown on demand)
     int adjSeeds = 0;
     DevBuf<double> adjPt, adjNode, adjRel;
+    // order-independent landings (option deterministic): per accumulator
+    // element an exponent and a 192-bit fixed-point sum
+    DevBuf<int> landExpo;
+    DevBuf<unsigned long long> landFix;
     bool gdenValid = false;
     double gdenLdefFact = 0.0, gdenAlpha = 0.0;
     int gdenMode = -1;
@@ -279,6 +284,7 @@ int validate_options(Ctx *c, const idw_options *o) {
         return fail(c, IDW_ERR_ARG, "walkLists must be IDW_WALK_LISTS_AUTO or IDW_WALK_LISTS_OFF");
     if (o->treeBuild != IDW_TREE_KD && o->treeBuild != IDW_TREE_MORTON)
         return fail(c, IDW_ERR_ARG, "treeBuild must be IDW_TREE_KD or IDW_TREE_MORTON");
+    if (o->deterministic != 0 && o->deterministic != 1) return fail(c, IDW_ERR_ARG, "deterministic must be 0 or 1");
     return IDW_OK;
 }
 
@@ -1403,6 +1409,101 @@ int idw_get_denominator(void *ctx, double *out, int64_t nvol, int where) {
     return copy_out(c, out, c->den.p, size_t(nvol), where);
 }
 
+}  // extern "C"
+
+// ---- order-independent landings (option deterministic, idw_land.cuh) ----
+
+// Deterministic reverse products run one at a time in the process: the
+// landing state is one constant per translation unit.
+std::mutex g_landMu;
+
+__global__ void k_land_convert(double *d, int64_t len, const int *expo, const unsigned long long *fix) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= len) return;
+    const int E = expo[t];
+    if (E == kLandNone) return;
+    if (E == kLandNonFinite) {
+        d[t] = __longlong_as_double(0x7ff8000000000000ll);
+        return;
+    }
+    unsigned long long u0 = fix[3 * t], u1 = fix[3 * t + 1], u2 = fix[3 * t + 2];
+    const bool neg = (u2 >> 63) != 0ull;
+    if (neg) {
+        u0 = ~u0 + 1ull;
+        const unsigned long long c0 = u0 == 0ull ? 1ull : 0ull;
+        u1 = ~u1 + c0;
+        const unsigned long long c1 = (c0 && u1 == 0ull) ? 1ull : 0ull;
+        u2 = ~u2 + c1;
+    }
+    // 2^E sits at bit 126
+    const double r = ldexp(double(u2), 2 + E) + ldexp(double(u1), E - 62) + ldexp(double(u0), E - 126);
+    d[t] += neg ? -r : r;
+}
+
+int land_set_all(Ctx *c, const LandState &s) {
+    cudaError_t e = land_set_adjoint(s, c->stream);
+    if (e == cudaSuccess) e = land_set_precise(s, c->stream);
+    if (e == cudaSuccess) e = land_set_walk(s, c->stream);
+    if (e == cudaSuccess) e = land_set_nodal(s, c->stream);
+    if (e == cudaSuccess) e = land_set_exact(s, c->stream);
+    if (e != cudaSuccess) return fail(c, IDW_ERR_CUDA, "landing state: %s", cudaGetErrorString(e));
+    return IDW_OK;
+}
+
+// Clears the landing state and waits for the stream when a deterministic
+// call ends, on every path out of it.
+struct LandClear {
+    Ctx *c;
+    bool on;
+    ~LandClear() {
+        if (!on) return;
+        LandState z{};
+        land_set_all(c, z);
+        cudaStreamSynchronize(c->stream);
+    }
+};
+
+// One scattering stage with order-independent landings into the nArr
+// accumulators (base[a], len[a] doubles): `stage(pass)` launches it, once
+// per pass; the fixed-point sums are then added to the accumulators.
+template <class F>
+int land_stage(Ctx *c, int nArr, double *const *base, const int64_t *len, F &&stage) {
+    int64_t total = 0;
+    for (int a = 0; a < nArr; ++a) total += len[a];
+    if (total <= 0) return stage(0);
+    CKA(c->landExpo.alloc(size_t(total)));
+    CKA(c->landFix.alloc(3 * size_t(total)));
+    CK(cudaMemsetAsync(c->landExpo.p, 0x80, sizeof(int) * size_t(total), c->stream));
+    CK(cudaMemsetAsync(c->landFix.p, 0, 3 * sizeof(unsigned long long) * size_t(total), c->stream));
+    LandState s{};
+    s.nArr = nArr;
+    int64_t off = 0;
+    for (int a = 0; a < nArr; ++a) {
+        s.base[a] = base[a];
+        s.len[a] = len[a];
+        s.expo[a] = c->landExpo.p + off;
+        s.fix[a] = c->landFix.p + 3 * off;
+        off += len[a];
+    }
+    for (int pass = 1; pass <= 2; ++pass) {
+        s.pass = pass;
+        if (int rc = land_set_all(c, s)) return rc;
+        if (int rc = stage(pass)) return rc;
+    }
+    LandState z{};
+    if (int rc = land_set_all(c, z)) return rc;
+    off = 0;
+    for (int a = 0; a < nArr; ++a) {
+        if (len[a] > 0)
+            k_land_convert<<<int((len[a] + 255) / 256), 256, 0, c->stream>>>(base[a], len[a], c->landExpo.p + off,
+                                                                              c->landFix.p + 3 * off);
+        off += len[a];
+    }
+    return check_launch(c, "order-independent landing");
+}
+
+extern "C" {
+
 static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStride, double *dxsOut, int where,
                      int64_t dxsStride) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
@@ -1436,57 +1537,109 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     CK(cudaMemsetAsync(ptAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * n, c->stream));
     CK(cudaMemsetAsync(nodeAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * nn, c->stream));
     CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
+    // deterministic: one such call at a time, the landing state cleared on every way out
+    const bool det = c->opt.deterministic != 0;
+    std::unique_lock<std::mutex> detLock;
+    if (det) detLock = std::unique_lock<std::mutex>(g_landMu);
+    LandClear landClear{c, det};
     CK(cudaEventRecord(c->ev0, c->stream));
+    const TreeDevF tf = tree_devf(c);
+    PointsDevF pf;
+    pf.da = c->ptDA.p;
+    pf.dl = c->ptDL.p;
+    pf.dm = c->ptDM.p;
+    pf.dml = c->ptDMl.p;
+    WalkRecF rec;
+    rec.hi = c->recHi.p;
+    rec.lo = c->recLo.p;
+    bool precise = false;
     if (mixed) {
-        const TreeDevF tf = tree_devf(c);
-        PointsDevF pf;
-        pf.da = c->ptDA.p;
-        pf.dl = c->ptDL.p;
-        pf.dm = c->ptDM.p;
-        pf.dml = c->ptDMl.p;
-        WalkRecF rec;
-        rec.hi = c->recHi.p;
-        rec.lo = c->recLo.p;
         rc = ensure_walk_lists(c, tf, rec, k);
         if (rc) return rc;
-        if (c->opt.adjointPrecision == IDW_ADJ_PRECISE && precise_adjoint_supported(k.law)) {
-            // the denominator to double-float accuracy: once per weight law and mode
-            if (!(c->denPValid && c->denPLdefFact == c->opt.LdefFact && c->denPAlpha == c->opt.alpha &&
-                  c->denPMode == c->opt.evalMode)) {
-                CKA(c->denP.alloc(size_t(c->nVol)));
-                launch_precise_denominator(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, c->denP.p, c->stream);
-                rc = check_launch(c, "precise denominator");
-                if (rc) return rc;
-                c->denPValid = true;
-                c->denPLdefFact = c->opt.LdefFact;
-                c->denPAlpha = c->opt.alpha;
-                c->denPMode = c->opt.evalMode;
-                CK(cudaEventRecord(c->ev0, c->stream));
-            }
+        precise = c->opt.adjointPrecision == IDW_ADJ_PRECISE && precise_adjoint_supported(k.law);
+        // the precise form's denominator to double-float accuracy: once per weight law and mode
+        if (precise && !(c->denPValid && c->denPLdefFact == c->opt.LdefFact && c->denPAlpha == c->opt.alpha &&
+                         c->denPMode == c->opt.evalMode)) {
+            CKA(c->denP.alloc(size_t(c->nVol)));
+            launch_precise_denominator(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, c->denP.p, c->stream);
+            rc = check_launch(c, "precise denominator");
+            if (rc) return rc;
+            c->denPValid = true;
+            c->denPLdefFact = c->opt.LdefFact;
+            c->denPAlpha = c->opt.alpha;
+            c->denPMode = c->opt.evalMode;
+            CK(cudaEventRecord(c->ev0, c->stream));
+        }
+    }
+    // the reverse walk: point and cluster moments land in ptAdj / nodeAdj
+    auto walk = [&](int) -> int {
+        if (mixed && precise)
             launch_adjoint_precise(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride,
-                                   c->denP.p, ptAdj.p, nodeAdj.p, n, c->counters.p, c->stream);
-            // the relative moments and the cluster shares, as the FP32 walk's
-            launch_adjoint_combine(tree_dev(c), c->ptXA.p, n, nSeeds, ptAdj.p, nodeAdj.p, ptRel.p, c->stream);
-        } else {
+                                   c->denP.p, ptAdj.p, nodeAdj.p, n, c->counters.p, c->stream, det);
+        else if (mixed)
             launch_adjoint_mixed(tree_dev(c), tf, pf, vol_dev(c), rec, k, exact, dxvDev, nSeeds, seedStride, c->den.p,
                                  ptAdj.p, nodeAdj.p, ptRel.p, c->ptXA.p, n, c->counters.p, c->stream,
-                                 c->adjMaxGroup);
-        }
+                                 c->adjMaxGroup, 0, det);
+        else
+            launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride,
+                                     ptAdj.p, nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p,
+                                     c->stream, det);
+        return check_launch(c, "adjoint walk");
+    };
+    if (det) {
+        // the second pass counts its work again: keep one pass's counters
+        double *base[2] = {ptAdj.p, nodeAdj.p};
+        const int64_t len[2] = {int64_t(nSeeds) * 12 * n, int64_t(nSeeds) * 12 * nn};
+        rc = land_stage(c, 2, base, len, [&](int pass) {
+            if (pass == 2) {
+                const cudaError_t e = cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream);
+                if (e != cudaSuccess) return fail(c, IDW_ERR_CUDA, "counters: %s", cudaGetErrorString(e));
+            }
+            return walk(pass);
+        });
     } else {
-        launch_walk_adjoint_fp64(tree_dev(c), p, vol_dev(c), k, exact, n, dxvDev, c->den.p, nSeeds, seedStride,
-                                 ptAdj.p, nodeAdj.p, int64_t(12) * n, int64_t(12) * nn, c->counters.p, c->stream);
+        rc = walk(0);
     }
+    if (rc) return rc;
+    // the relative moments and the cluster shares (setData_b folded in)
+    if (mixed) launch_adjoint_combine(tree_dev(c), c->ptXA.p, n, nSeeds, ptAdj.p, nodeAdj.p, ptRel.p, c->stream);
     CK(cudaEventRecord(c->ev1, c->stream));
     c->eventsRecorded = true;
     rc = check_launch(c, "adjoint walk");
     if (rc) return rc;
     SurfaceDev s = surf_dev(c);
+    const bool faceLandings = c->opt.useRotations && c->nFaces > 0;
     for (int sd = 0; sd < nSeeds; ++sd) {
         double *pa = (mixed ? ptRel.p : ptAdj.p) + size_t(sd) * 12 * n;
         if (!mixed) launch_set_data_b(tree_dev(c), nodeAdj.p + size_t(sd) * 12 * nn, pa, n, c->stream);
         CK(cudaMemsetAsync(c->xub.p, 0, sizeof(double) * 3 * n, c->stream));
-        launch_nodal_b(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa, mixed,
-                       c->xub.p, c->stream, sd == 0);
+        if (det && faceLandings) {
+            // node part: area and normal adjoints land in the faces' scratch
+            // (Xub += Bb is the node's own write: from zero in each pass)
+            double *faceAdj[1] = {c->faceScratch.p + 4 * size_t(c->nFaces)};
+            const int64_t faceLen[1] = {4 * int64_t(c->nFaces)};
+            rc = land_stage(c, 1, faceAdj, faceLen, [&](int pass) {
+                if (pass == 2) {
+                    const cudaError_t e = cudaMemsetAsync(c->xub.p, 0, sizeof(double) * 3 * n, c->stream);
+                    if (e != cudaSuccess) return fail(c, IDW_ERR_CUDA, "Xub: %s", cudaGetErrorString(e));
+                }
+                launch_nodal_b_nodes(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa,
+                                     mixed, c->xub.p, c->stream, sd == 0 && pass <= 1, 1);
+                return check_launch(c, "reverse nodal properties");
+            });
+            if (rc) return rc;
+            // face part: each face's element adjoint lands in Xub of its vertices
+            double *xubArr[1] = {c->xub.p};
+            const int64_t xubLen[1] = {3 * int64_t(n)};
+            rc = land_stage(c, 1, xubArr, xubLen, [&](int) {
+                launch_nodal_b_faces(s, c->xu.p, c->opt.useRotations, c->xub.p, c->stream, 1);
+                return check_launch(c, "reverse nodal properties");
+            });
+            if (rc) return rc;
+        } else {
+            launch_nodal_b(s, c->xu.p, c->ptXA.p, c->normals0.p, c->isCorner.p, c->opt.useRotations, pa, mixed,
+                           c->xub.p, c->stream, sd == 0);
+        }
         double *dst = (where == IDW_DEVICE) ? dxsOut + sd * dxsStride : c->dxs.p;
         CK(cudaMemsetAsync(dst, 0, sizeof(double) * 3 * c->nPts, c->stream));
         launch_scatter_dxs(n, c->xuInd.p, c->xub.p, dst, c->stream);

@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(kThreads) k_exact_mixed2(TreeDevF tf, PointsDe
 // slot 3 a + k: w (r - C)_k n_a, C the leaf centroid), the layout the adjoint
 // walk writes.  Each thread sums its NV nodes' products per point; the warp
 // reduces them (warp_land_moments) and lands one FP64 atomic per moment.
-template <int KIND, int NV>
+template <int KIND, int NV, bool DET = false>
 __global__ void __launch_bounds__(kThreads) k_exact_adjoint(TreeDevF tf, PointsDevF pf, VolumeDev v, WalkRecF rec,
                                                             MixedParams mp, Law32<KIND> law, const double *dxv,
                                                             const double *den, double *ptAdj,
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(kThreads) k_exact_adjoint(TreeDevF tf, PointsD
                             P[9 + a] = fmaf(wn, R[j][2], P[9 + a]);
                         }
                     }
-                    warp_land_moments(P, ptAdj + 12 * int64_t(p0 + t));
+                    warp_land_moments<DET>(P, ptAdj + 12 * int64_t(p0 + t));
                 }
                 p = e;
                 if (e == L.y + 1) {
@@ -558,11 +558,21 @@ void launch_kind(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF &af, c
 
 void launch_exact_adjoint(const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
                           const MixedParams &mp, const WeightLaw &wl, const double *dxv, const double *den,
-                          double *ptAdj, unsigned long long *counters, cudaStream_t st) {
+                          double *ptAdj, unsigned long long *counters, cudaStream_t st, int det) {
     if (v.nVol <= 0 || tf.nPts <= 0 || tf.nLeaves <= 0) return;
     constexpr int NV = 4;
     const int grid = blocks_for(v.nVol, kThreads * NV);
-    if (wl.isInt && wl.ia == 3 && wl.ib == 5) {
+    if (det) {  // order-independent landings (idw_land.cuh)
+        if (wl.isInt && wl.ia == 3 && wl.ib == 5)
+            k_exact_adjoint<0, NV, true><<<grid, kThreads, 0, st>>>(tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, dxv,
+                                                                    den, ptAdj, counters);
+        else if (wl.isInt)
+            k_exact_adjoint<1, NV, true><<<grid, kThreads, 0, st>>>(
+                tf, pf, v, rec, mp, Law32<1>{wl.ia, wl.ib, float(wl.aExp), float(wl.bExp)}, dxv, den, ptAdj, counters);
+        else
+            k_exact_adjoint<2, NV, true><<<grid, kThreads, 0, st>>>(
+                tf, pf, v, rec, mp, Law32<2>{0, 0, float(wl.aExp), float(wl.bExp)}, dxv, den, ptAdj, counters);
+    } else if (wl.isInt && wl.ia == 3 && wl.ib == 5) {
         k_exact_adjoint<0, NV><<<grid, kThreads, 0, st>>>(tf, pf, v, rec, mp, Law32<0>{3, 5, 3.f, 5.f}, dxv, den,
                                                           ptAdj, counters);
     } else if (wl.isInt) {
@@ -590,5 +600,7 @@ void launch_exact_mixed(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF
         launch_kind<2>(tf, pf, af, v, rec, mp, Law32<2>{0, 0, float(wl.aExp), float(wl.bExp)}, acc, counters, st);
     }
 }
+
+IDW_LAND_SETTER(land_set_exact)
 
 }  // namespace idw

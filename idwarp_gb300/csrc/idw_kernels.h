@@ -223,7 +223,7 @@ void launch_exact_mixed(const TreeDevF &tf, const PointsDevF &pf, const NodeAggF
 // caller), tiled as launch_exact_mixed (idw_exact.cu).
 void launch_exact_adjoint(const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v, const WalkRecF &rec,
                           const MixedParams &mp, const WeightLaw &wl, const double *dxv, const double *den,
-                          double *ptAdj, unsigned long long *counters, cudaStream_t st);
+                          double *ptAdj, unsigned long long *counters, cudaStream_t st, int det = 0);
 // True when the tiled exact kernel has volume nodes for at least two full
 // waves of the device (below that the walk's finer grain is faster).
 bool exact_tiled_fills(int64_t nVol);
@@ -232,7 +232,7 @@ void launch_gate_den(int64_t nVol, const float4 *acc, float *gden, cudaStream_t 
 int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,
                              int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,
                              double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
-                             unsigned long long *counters, cudaStream_t st);
+                             unsigned long long *counters, cudaStream_t st, int det = 0);
 MixedParams make_mixed_params(const EvalConsts &k);
 // Largest number of surfaces that share one batched walk.
 #ifndef IDW_BATCH_MAX
@@ -253,7 +253,7 @@ int launch_adjoint_mixed(const TreeDev &t, const TreeDevF &tf, const PointsDevF 
                          const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                          int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, double *ptAdj,
                          const dbl4 *ptXA, int nPts, unsigned long long *counters, cudaStream_t st,
-                         int maxGroup = 16);
+                         int maxGroup = 16, int combine = 1, int det = 0);
 // Point and cluster moments of a mixed reverse walk -> the relative point
 // adjoints of the reverse nodal properties (setData_b folded in).
 void launch_adjoint_combine(const TreeDev &t, const dbl4 *ptXA, int nPts, int nSeeds, const double *ptAcc,
@@ -267,9 +267,26 @@ void launch_precise_denominator(const TreeDev &t, const TreeDevF &tf, const Poin
 int launch_adjoint_precise(const TreeDev &t, const TreeDevF &tf, const PointsDevF &pf, const VolumeDev &v,
                            const WalkRecF &rec, const EvalConsts &k, int exact, const double *dxv, int nSeeds,
                            int64_t dxvStride, const double *den, double *ptAcc, double *nodeAcc, int nPts,
-                           unsigned long long *counters, cudaStream_t st);
+                           unsigned long long *counters, cudaStream_t st, int det = 0);
 int sort_morton(int64_t nVol, unsigned long long *codes, int *idx, unsigned long long *codesAlt, int *perm,
                 cudaStream_t st);
+
+// Setters of the landing state (idw_land.cuh), one per translation unit
+// that lands FP64 sums; set all of them on the launching stream.
+struct LandState;
+cudaError_t land_set_adjoint(const LandState &s, cudaStream_t st);
+cudaError_t land_set_precise(const LandState &s, cudaStream_t st);
+cudaError_t land_set_walk(const LandState &s, cudaStream_t st);
+cudaError_t land_set_nodal(const LandState &s, cudaStream_t st);
+cudaError_t land_set_exact(const LandState &s, cudaStream_t st);
+// The nodal adjoint's two parts (launch_nodal_b runs both): nodes, whose
+// area and normal adjoints land in the faces' scratch, then faces, whose
+// element adjoints land in Xub; det: order-independent landings.
+void launch_nodal_b_nodes(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
+                          const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
+                          cudaStream_t st, int faceProps, int det);
+void launch_nodal_b_faces(const SurfaceDev &s, const double *Xu, int useRotations, double *Xub, cudaStream_t st,
+                          int det);
 
 // Surface tree built on the device (idw_tree.cu): Morton order, binary radix
 // tree cut at bucket-size leaves, in the host kd build's layout.  pts: host

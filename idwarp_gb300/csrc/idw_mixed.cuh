@@ -4,6 +4,7 @@
 #pragma once
 #include "idw_common.cuh"
 #include "idw_kernels.h"
+#include "idw_land.cuh"
 
 namespace idw {
 
@@ -381,6 +382,7 @@ __device__ __forceinline__ int resolve64(int dec, const TreeDev &t, const Volume
 // halving exchanges (xor 16, 8) leave lane group G = lane >> 3 with the 3
 // products of moment G; three butterflies (xor 4, 2, 1) complete the sums;
 // lanes 0..2 of each group land them.  Called by all 32 lanes.
+template <bool DET>
 __device__ __forceinline__ void warp_land_moments(const float *P, double *d) {
     const int lane = threadIdx.x & 31;
     const bool h16 = lane & 16, h8 = lane & 8;
@@ -403,7 +405,7 @@ __device__ __forceinline__ void warp_land_moments(const float *P, double *d) {
     const int G = lane >> 3, a = lane & 7;
     if (a < 3) {
         const float val = a == 0 ? R[0] : (a == 1 ? R[1] : R[2]);
-        if (val != 0.f) atomicAdd(d + (G == 0 ? 9 + a : 3 * a + G - 1), double(val));
+        if (val != 0.f) land_add<DET>(d + (G == 0 ? 9 + a : 3 * a + G - 1), double(val));
     }
 }
 

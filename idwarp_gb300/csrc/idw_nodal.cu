@@ -13,6 +13,7 @@
 // registers instead of replaying a tape.
 #include "idw_common.cuh"
 #include "idw_kernels.h"
+#include "idw_land.cuh"
 #include "idw_nodal_math.cuh"
 
 namespace idw {
@@ -21,6 +22,7 @@ namespace {
 
 // Adjoint of element_props: accumulate d(area)*areab + d(normal).normalb into
 // Xub of the face's vertices (atomically: vertices are shared between nodes).
+template <bool DET>
 __device__ void element_props_b(const double *Xu, const int *conn, int np, double areab, const double *normalb,
                                 double *Xub) {
     double c[3] = {0, 0, 0};
@@ -93,9 +95,9 @@ __device__ void element_props_b(const double *Xu, const int *conn, int np, doubl
     cb[2] /= double(np);
     for (int k = 0; k < np; ++k) {
         double *o = Xub + 3 * conn[k];
-        atomicAdd(o + 0, rvb[k][0] + cb[0]);
-        atomicAdd(o + 1, rvb[k][1] + cb[1]);
-        atomicAdd(o + 2, rvb[k][2] + cb[2]);
+        land_add<DET>(o + 0, rvb[k][0] + cb[0]);
+        land_add<DET>(o + 1, rvb[k][1] + cb[1]);
+        land_add<DET>(o + 2, rvb[k][2] + cb[2]);
     }
 }
 
@@ -341,6 +343,7 @@ __global__ void k_set_data_b(TreeDev t, const double *nodeAdj, double *ptAdj, in
 // and from it the adjoints of the face areas and normals it was summed from,
 // added per face (the face part then runs each face's element adjoint once:
 // element_props_b is linear in those adjoints).
+template <bool DET>
 __global__ void k_nodal_b_nodes(SurfaceDev s, const dbl4 *xa, const double *normals0, const int *isCorner,
                                 int useRotations, const double *ptAdj, int relative, double *Xub) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -375,15 +378,16 @@ __global__ void k_nodal_b_nodes(SurfaceDev s, const dbl4 *xa, const double *norm
         const double dA = fp[0] / double(np);
         const double dAb = sab + fp[1] * snb[0] + fp[2] * snb[1] + fp[3] * snb[2];
         double *fa = faceAdj + 4 * int64_t(f);
-        atomicAdd(fa + 0, dAb / double(np));
-        atomicAdd(fa + 1, dA * snb[0]);
-        atomicAdd(fa + 2, dA * snb[1]);
-        atomicAdd(fa + 3, dA * snb[2]);
+        land_add<DET>(fa + 0, dAb / double(np));
+        land_add<DET>(fa + 1, dA * snb[0]);
+        land_add<DET>(fa + 2, dA * snb[1]);
+        land_add<DET>(fa + 3, dA * snb[2]);
     }
 }
 
 // Reverse nodal properties, face part: each face's element adjoint with the
 // summed area and normal adjoints of its nodes, into Xub of its vertices.
+template <bool DET>
 __global__ void k_nodal_b_faces(SurfaceDev s, const double *Xu, double *Xub) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= s.nFaces) return;
@@ -391,7 +395,7 @@ __global__ void k_nodal_b_faces(SurfaceDev s, const double *Xu, double *Xub) {
     const double areab = fa[0], nb[3] = {fa[1], fa[2], fa[3]};
     if (areab == 0.0 && nb[0] == 0.0 && nb[1] == 0.0 && nb[2] == 0.0) return;
     const int f0 = s.facePtr[f], np = s.facePtr[f + 1] - f0;
-    element_props_b(Xu, s.faceConn + f0, np, areab, nb, Xub);
+    element_props_b<DET>(Xu, s.faceConn + f0, np, areab, nb, Xub);
 }
 
 // dXs[XuInd[i]] = Xub[i]: only the first caller occurrence of a unique point
@@ -599,8 +603,30 @@ void launch_nodal_b(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const
         if (faceProps) k_face_props<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu);
         cudaMemsetAsync(s.faceScratch + 4 * size_t(s.nFaces), 0, 4 * sizeof(double) * size_t(s.nFaces), st);
     }
-    k_nodal_b_nodes<<<blocks(s.n, 128), 128, 0, st>>>(s, xa, normals0, isCorner, useRotations, ptAdj, relative, Xub);
-    if (useRotations && s.nFaces > 0) k_nodal_b_faces<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu, Xub);
+    k_nodal_b_nodes<false>
+        <<<blocks(s.n, 128), 128, 0, st>>>(s, xa, normals0, isCorner, useRotations, ptAdj, relative, Xub);
+    if (useRotations && s.nFaces > 0) k_nodal_b_faces<false><<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu, Xub);
+}
+void launch_nodal_b_nodes(const SurfaceDev &s, const double *Xu, const dbl4 *xa, const double *normals0,
+                          const int *isCorner, int useRotations, const double *ptAdj, int relative, double *Xub,
+                          cudaStream_t st, int faceProps, int det) {
+    if (s.n <= 0) return;
+    if (useRotations && s.nFaces > 0) {
+        if (faceProps) k_face_props<<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu);
+        cudaMemsetAsync(s.faceScratch + 4 * size_t(s.nFaces), 0, 4 * sizeof(double) * size_t(s.nFaces), st);
+    }
+    if (det)
+        k_nodal_b_nodes<true>
+            <<<blocks(s.n, 128), 128, 0, st>>>(s, xa, normals0, isCorner, useRotations, ptAdj, relative, Xub);
+    else
+        k_nodal_b_nodes<false>
+            <<<blocks(s.n, 128), 128, 0, st>>>(s, xa, normals0, isCorner, useRotations, ptAdj, relative, Xub);
+}
+void launch_nodal_b_faces(const SurfaceDev &s, const double *Xu, int useRotations, double *Xub, cudaStream_t st,
+                          int det) {
+    if (!(s.n > 0 && useRotations && s.nFaces > 0)) return;
+    if (det) k_nodal_b_faces<true><<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu, Xub);
+    else k_nodal_b_faces<false><<<blocks(s.nFaces, 128), 128, 0, st>>>(s, Xu, Xub);
 }
 void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, const dbl4 *xa, const double *normals0,
                     const double *Ai, const int *isCorner, int useRotations, int plusIdentity, double *ptMBd,
@@ -612,5 +638,7 @@ void launch_nodal_d(const SurfaceDev &s, const double *Xu, const double *Xud, co
 void launch_scatter_dxs(int n, const int *xuInd, const double *Xub, double *dXs, cudaStream_t st) {
     if (n > 0) k_scatter_dxs<<<blocks(n, 256), 256, 0, st>>>(n, xuInd, Xub, dXs);
 }
+
+IDW_LAND_SETTER(land_set_nodal)
 
 }  // namespace idw

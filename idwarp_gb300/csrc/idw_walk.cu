@@ -20,6 +20,7 @@
 // same for all 32 lanes (broadcast loads).
 #include "idw_common.cuh"
 #include "idw_kernels.h"
+#include "idw_land.cuh"
 
 namespace idw {
 
@@ -160,17 +161,18 @@ __global__ void __launch_bounds__(128) k_walk64(TreeDev t, PointsDev p, VolumeDe
 }
 
 // Sum `val` over the lanes of the warp and add it to *dst from lane 0.
+template <bool DET>
 __device__ __forceinline__ void warp_atomic_add(double *dst, double val, bool any) {
     if (!any) return;
     double s = warp_sum(val);
-    if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(dst, s);
+    if ((threadIdx.x & 31) == 0 && s != 0.0) land_add<DET>(dst, s);
 }
 
 
 // Reverse walk for nSeeds seeds at once: the weights are computed once per
 // pair and shared by all seeds.  Point adjoints are 12 values per point per
 // seed (Mib row-major then Bib), cluster adjoints likewise per tree node.
-template <int NS>
+template <int NS, bool DET = false>
 __global__ void __launch_bounds__(128) k_walk_adj64(TreeDev t, PointsDev p, VolumeDev v, EvalConsts k, int exact,
                                                     int nPts, const double *dxv, const double *den, int64_t seedStride,
                                                     double *ptAdj, double *nodeAdj, int64_t ptStride,
@@ -227,8 +229,8 @@ __global__ void __launch_bounds__(128) k_walk_adj64(TreeDev t, PointsDev p, Volu
 #pragma unroll
                             for (int a = 0; a < 3; ++a) {
 #pragma unroll
-                                for (int c = 0; c < 3; ++c) warp_atomic_add(dst + 3 * a + c, r[c] * sib[a], true);
-                                warp_atomic_add(dst + 9 + a, sib[a], true);
+                                for (int c = 0; c < 3; ++c) warp_atomic_add<DET>(dst + 3 * a + c, r[c] * sib[a], true);
+                                warp_atomic_add<DET>(dst + 9 + a, sib[a], true);
                             }
                         }
                     }
@@ -266,8 +268,8 @@ __global__ void __launch_bounds__(128) k_walk_adj64(TreeDev t, PointsDev p, Volu
 #pragma unroll
                         for (int a = 0; a < 3; ++a) {
 #pragma unroll
-                            for (int c = 0; c < 3; ++c) warp_atomic_add(dst + 3 * a + c, r[c] * sib[a], true);
-                            warp_atomic_add(dst + 9 + a, sib[a], true);
+                            for (int c = 0; c < 3; ++c) warp_atomic_add<DET>(dst + 3 * a + c, r[c] * sib[a], true);
+                            warp_atomic_add<DET>(dst + 9 + a, sib[a], true);
                         }
                     }
                 }
@@ -287,11 +289,11 @@ void launch_walk_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, 
     if (v.nVol > 0) k_walk64<<<blocks(v.nVol, 128), 128, 0, st>>>(t, p, v, nodeMB, k, exact, nPts, o);
 }
 
-int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,
-                             int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,
-                             double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
-                             unsigned long long *counters, cudaStream_t st) {
-    if (v.nVol <= 0) return 0;
+template <bool DET>
+void launch_adj64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact, int nPts,
+                  const double *dxv, const double *den, int nSeeds, int64_t seedStride, double *ptAdj,
+                  double *nodeAdj, int64_t ptStride, int64_t nodeStride, unsigned long long *counters,
+                  cudaStream_t st) {
     const int g = blocks(v.nVol, 128);
     // Seeds are processed in groups of 1, 4 or 16 sharing one walk.
     int s0 = 0;
@@ -301,20 +303,36 @@ int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeD
         double *pa = ptAdj + s0 * ptStride;
         double *na = nodeAdj + s0 * nodeStride;
         if (left >= 16) {
-            k_walk_adj64<16><<<g, 128, 0, st>>>(t, p, v, k, exact, nPts, d, den, seedStride, pa, na, ptStride,
-                                                nodeStride, counters);
+            k_walk_adj64<16, DET><<<g, 128, 0, st>>>(t, p, v, k, exact, nPts, d, den, seedStride, pa, na, ptStride,
+                                                     nodeStride, counters);
             s0 += 16;
         } else if (left >= 4) {
-            k_walk_adj64<4><<<g, 128, 0, st>>>(t, p, v, k, exact, nPts, d, den, seedStride, pa, na, ptStride,
-                                               nodeStride, counters);
+            k_walk_adj64<4, DET><<<g, 128, 0, st>>>(t, p, v, k, exact, nPts, d, den, seedStride, pa, na, ptStride,
+                                                    nodeStride, counters);
             s0 += 4;
         } else {
-            k_walk_adj64<1><<<g, 128, 0, st>>>(t, p, v, k, exact, nPts, d, den, seedStride, pa, na, ptStride,
-                                               nodeStride, counters);
+            k_walk_adj64<1, DET><<<g, 128, 0, st>>>(t, p, v, k, exact, nPts, d, den, seedStride, pa, na, ptStride,
+                                                    nodeStride, counters);
             s0 += 1;
         }
     }
+}
+
+int launch_walk_adjoint_fp64(const TreeDev &t, const PointsDev &p, const VolumeDev &v, const EvalConsts &k, int exact,
+                             int nPts, const double *dxv, const double *den, int nSeeds, int64_t seedStride,
+                             double *ptAdj, double *nodeAdj, int64_t ptStride, int64_t nodeStride,
+                             unsigned long long *counters, cudaStream_t st, int det) {
+    if (v.nVol <= 0) return 0;
+    // det: order-independent landings (idw_land.cuh)
+    if (det)
+        launch_adj64<true>(t, p, v, k, exact, nPts, dxv, den, nSeeds, seedStride, ptAdj, nodeAdj, ptStride,
+                           nodeStride, counters, st);
+    else
+        launch_adj64<false>(t, p, v, k, exact, nPts, dxv, den, nSeeds, seedStride, ptAdj, nodeAdj, ptStride,
+                            nodeStride, counters, st);
     return 0;
 }
+
+IDW_LAND_SETTER(land_set_walk)
 
 }  // namespace idw

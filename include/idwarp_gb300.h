@@ -101,7 +101,13 @@ typedef struct idw_options {
                            * a leaf) and replayed by every later warp; same sums either way */
     int32_t treeBuild;    /* IDW_TREE_KD (default) or IDW_TREE_MORTON; read by
                            * idw_initialize_warping, as bucketSize */
-    int32_t reserved[3];
+    int32_t deterministic; /* 0 (default): reverse products (idw_warp_deriv*) land their sums with
+                            * FP64 atomics, whose order varies from run to run; 1: every scattering
+                            * stage runs twice and lands order-independent 192-bit fixed-point sums,
+                            * so dXs is the same bit for bit on every run (about twice the time;
+                            * such calls are serialised within the process).  The forward calls are
+                            * deterministic either way. */
+    int32_t reserved[2];
 } idw_options;
 
 /* Work counters of the last warp / warpDeriv call. */

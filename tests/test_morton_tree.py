@@ -111,11 +111,12 @@ def test_struct_sizes_match_header(tmp_path):
     inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "idwarp_gb300.h"\n'
-                   'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(idw_options), sizeof(idw_stats), '
-                   'sizeof(idw_tuning), offsetof(idw_options, treeBuild), offsetof(idw_stats, treeBuildMs)); '
-                   'return 0; }\n')
+                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(idw_options), sizeof(idw_stats), '
+                   'sizeof(idw_tuning), offsetof(idw_options, treeBuild), offsetof(idw_stats, treeBuildMs), '
+                   'offsetof(idw_options, deterministic)); return 0; }\n')
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-I", inc, str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert got == [C.sizeof(_lib.idw_options), C.sizeof(_lib.idw_stats), C.sizeof(_lib.idw_tuning),
-                   _lib.idw_options.treeBuild.offset, _lib.idw_stats.treeBuildMs.offset]
+                   _lib.idw_options.treeBuild.offset, _lib.idw_stats.treeBuildMs.offset,
+                   _lib.idw_options.deterministic.offset]
