@@ -57,12 +57,14 @@ def make_workload(cfg, seed=2):
 
 WALK_LISTS = "auto"  # --walk-lists: "off" makes every walk decide as it goes
 TREE_BUILD = "kd"  # --tree-build: "morton" builds the surface tree on the GPU
+DETERMINISTIC = False  # --deterministic: reverse products with order-independent sums
 
 
 def mesh_options(m, precision, mode="fast", tree=None):
     return {"fileType": "NPY", "precision": precision, "evalMode": mode, "errTol": ERR_TOL,
             "aExp": 3.0, "bExp": 5.0, "LdefFact": 1.0, "alpha": 0.25, "bucketSize": 8,
-            "symmetryPlanes": m["symmetryPlanes"], "walkLists": WALK_LISTS, "treeBuild": tree or TREE_BUILD}
+            "symmetryPlanes": m["symmetryPlanes"], "walkLists": WALK_LISTS, "treeBuild": tree or TREE_BUILD,
+            "deterministic": DETERMINISTIC}
 
 
 def build_mesh(m, precision, mode="fast", restartFile=None):
@@ -698,27 +700,48 @@ def run_case(case, cfg, reps):
         sd = torch.tensor(np.random.default_rng(100).normal(size=(ns, nvol, 3)), device="cuda")
         npts = len(m["xs"])
         out = torch.zeros((ns, npts, 3), dtype=torch.float64, device="cuda")
-        for _ in range(reps):
+
+        def deriv():
             if ns == 1:
                 rc = L.idw_warp_deriv(mesh.ctx, C.c_void_p(sd.data_ptr()), 3 * nvol, _lib.IDW_DEVICE)
             else:
                 rc = L.idw_warp_deriv_batch(mesh.ctx, C.c_void_p(sd.data_ptr()), ns, C.c_void_p(out.data_ptr()),
                                             _lib.IDW_DEVICE)
             _lib.check(L, mesh.ctx, rc, "warpDeriv")
-    elif case == "batch":
+            return (mesh.getdXs().copy() if ns == 1 else out.cpu().numpy().copy())
+
+        stream = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        first = deriv()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            deriv()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        again = deriv()
+        scale = float(np.abs(first).max())
+        extra = {"ms_per_call": e0.elapsed_time(e1) / max(reps, 1), "deterministic": DETERMINISTIC,
+                 "repeat_bitwise_equal": bool(np.array_equal(first, again)),
+                 "repeat_max_diff_over_max_dXs": float(np.abs(first - again).max() / scale)}
+    else:
+        extra = {}
+    if case == "batch":
         sb = torch.tensor(np.stack([S.wing_perturbation(m["pts"], seed=200 + i) for i in range(8)]), device="cuda")
         ob = torch.empty((8, nvol, 3), dtype=torch.float64, device="cuda")
         for _ in range(reps):
             _lib.check(L, mesh.ctx, L.idw_warp_mesh_batch(mesh.ctx, C.c_void_p(sb.data_ptr()), 8,
                                                           C.c_void_p(ob.data_ptr()), _lib.IDW_DEVICE),
                        "warpMeshBatch")
-    else:
+    elif case == "warp":
         for _ in range(reps):
             mesh.warpMesh()
     torch.cuda.synchronize()
     st = mesh.getStats()
-    print(json.dumps({"case": case, "config": cfg, "reps": reps, "lastKernelMs": st["lastKernelMs"],
-                      "walkListEntries": st["walkListEntries"]}))
+    line = {"case": case, "config": cfg, "reps": reps, "lastKernelMs": st["lastKernelMs"],
+            "walkListEntries": st["walkListEntries"]}
+    line.update(extra)
+    print(json.dumps(line))
     return 0
 
 
@@ -737,6 +760,8 @@ def main():
     ap.add_argument("--suite-d", action="store_true", help="the 20M-node two-body FFD loop")
     ap.add_argument("--suite-tree", action="store_true",
                     help="error report of the GPU-built Morton tree against the kd tree (S1, W errTol sweep, P)")
+    ap.add_argument("--deterministic", action="store_true",
+                    help="reverse products with order-independent sums (bitwise repeatable dXs)")
     ap.add_argument("--tree-build", default="kd", choices=["kd", "morton"],
                     help="surface tree: the reference's kd tree (host) or the Morton tree (GPU)")
     ap.add_argument("--walk-lists", default="auto", choices=["auto", "off"],
@@ -744,9 +769,10 @@ def main():
     ap.add_argument("--case", choices=["warp", "deriv1", "deriv1fast", "deriv16", "deriv16fast", "batch", "setup"],
                     help="run one operation --steps times on --config's mesh (the small profiling cases)")
     args = ap.parse_args()
-    global WALK_LISTS, TREE_BUILD
+    global WALK_LISTS, TREE_BUILD, DETERMINISTIC
     WALK_LISTS = args.walk_lists
     TREE_BUILD = args.tree_build
+    DETERMINISTIC = args.deterministic
     if args.case:
         import torch
 
