@@ -1507,6 +1507,14 @@ extern "C" {
 static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStride, double *dxsOut, int where,
                      int64_t dxsStride) {
     if (!c->haveTree) return fail(c, IDW_ERR_STATE, "setSurfaceDefinition must come first");
+    const bool det = c->opt.deterministic != 0;
+    if (det) {
+        // the passes set constant memory and wait for the stream: not inside a capture
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(c->stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(c, IDW_ERR_STATE, "deterministic reverse products cannot be captured in a CUDA graph");
+    }
     if (int e0 = ensure_den0(c)) return e0;
     if (!c->haveWarp) return fail(c, IDW_ERR_STATE, "warpMesh must be called before warpDeriv");
     int rc = refresh_nodal(c);
@@ -1538,7 +1546,6 @@ static int run_deriv(Ctx *c, const double *dxvDev, int nSeeds, int64_t seedStrid
     CK(cudaMemsetAsync(nodeAdj.p, 0, sizeof(double) * size_t(nSeeds) * 12 * nn, c->stream));
     CK(cudaMemsetAsync(c->counters.p, 0, 8 * sizeof(unsigned long long), c->stream));
     // deterministic: one such call at a time, the landing state cleared on every way out
-    const bool det = c->opt.deterministic != 0;
     std::unique_lock<std::mutex> detLock;
     if (det) detLock = std::unique_lock<std::mutex>(g_landMu);
     LandClear landClear{c, det};

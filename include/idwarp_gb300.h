@@ -105,8 +105,9 @@ typedef struct idw_options {
                             * FP64 atomics, whose order varies from run to run; 1: every scattering
                             * stage runs twice and lands order-independent 192-bit fixed-point sums,
                             * so dXs is the same bit for bit on every run (about twice the time;
-                            * such calls are serialised within the process; idw_warp_deriv_noalloc
-                            * keeps the atomics).  The forward calls are deterministic either way. */
+                            * such calls are serialised within the process, wait for the stream and
+                            * refuse stream capture (IDW_ERR_STATE); idw_warp_deriv_noalloc keeps the
+                            * atomics).  The forward calls are deterministic either way. */
     int32_t reserved[2];
 } idw_options;
 

@@ -101,3 +101,31 @@ def test_option_switches_at_run_time(built_lib):
     d2 = _deriv(g, dxv, 1)
     np.testing.assert_array_equal(d1, d2)
     assert np.abs(d1 - a).max() <= 1e-12 * np.abs(a).max()
+
+
+def test_capture_refused(built_lib):
+    # the passes wait for the stream: a deterministic call inside a CUDA graph
+    # capture returns IDW_ERR_STATE before it enqueues anything
+    import ctypes as C
+
+    import torch
+
+    from idwarp_gb300 import _lib
+
+    m = wing_small()
+    g = build_gpu(m, {"deterministic": True}, precision="mixed")
+    g.setSurfaceCoordinates(m["xs"])
+    g.warpMesh()
+    nv, ns = len(m["xv0"]), len(m["pts"])
+    seeds = torch.zeros((1, nv, 3), dtype=torch.float64, device="cuda")
+    dxs = torch.empty((1, ns, 3), dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    g.lib.idw_set_stream(g.ctx, C.c_void_p(s.cuda_stream))
+    graph = torch.cuda.CUDAGraph()
+    rc = None
+    with torch.cuda.graph(graph, stream=s):
+        rc = g.lib.idw_warp_deriv_batch(g.ctx, C.c_void_p(seeds.data_ptr()), 1, C.c_void_p(dxs.data_ptr()),
+                                        _lib.IDW_DEVICE)
+        torch.zeros(1, device="cuda")  # the graph holds one node of its own
+    assert rc == _lib.IDW_ERR_STATE
+    torch.cuda.synchronize()
