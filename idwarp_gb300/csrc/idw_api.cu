@@ -1451,14 +1451,19 @@ int land_set_all(Ctx *c, const LandState &s) {
 }
 
 // Clears the landing state and waits for the stream when a deterministic
-// call ends, on every path out of it.
+// call ends, on every path out of it (quietly: an error that ended the call
+// keeps its message).
 struct LandClear {
     Ctx *c;
     bool on;
     ~LandClear() {
         if (!on) return;
         LandState z{};
-        land_set_all(c, z);
+        land_set_adjoint(z, c->stream);
+        land_set_precise(z, c->stream);
+        land_set_walk(z, c->stream);
+        land_set_nodal(z, c->stream);
+        land_set_exact(z, c->stream);
         cudaStreamSynchronize(c->stream);
     }
 };
