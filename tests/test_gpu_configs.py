@@ -10,6 +10,8 @@
   volume nodes are independent given the surface, so the sample's oracle
   result is the full mesh's at those nodes); GPU meshes of just the sampled
   nodes give the decision counts for the same nodes.
+* Both with the reference's kd tree and with the GPU-built Morton tree
+  (option treeBuild "morton", against the oracle's restatement of it).
 
 Bars: FP64 1e-12 Ldef, mixed 1e-8 Ldef (max over nodes of the largest
 coordinate error), widened to 4x the case's rounding sensitivity where that
@@ -75,13 +77,16 @@ def w():
     return m
 
 
+@pytest.mark.parametrize("tree", ["kd", "morton"])
 @pytest.mark.parametrize("mode", ["fast", "exact"])
-def test_s1_warp_matches_oracle(mode, s1, built_lib, oracle_lib):
+def test_s1_warp_matches_oracle(mode, tree, s1, built_lib, oracle_lib):
+    # tree "morton": the GPU-built tree against the oracle's restatement of it
     assert len(s1["xv0"]) == 95354 and len(s1["pts"]) == 2166
-    om, xo, L, sens = _sensitivity(s1, {"evalMode": mode})
+    opts = {"evalMode": mode, "treeBuild": tree}
+    om, xo, L, sens = _sensitivity(s1, opts)
     so = om.stats()
     for prec in ("fp64", "mixed"):
-        g = build_gpu(s1, {"evalMode": mode}, precision=prec)
+        g = build_gpu(s1, opts, precision=prec)
         g.setSurfaceCoordinates(s1["xs"])
         g.warpMesh()
         err = np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / L
@@ -109,17 +114,18 @@ def test_s1_warp_deriv(mode, s1, built_lib, oracle_lib):
     assert np.abs(out["mixed"] - out["fp64"]).max() <= TOL_DERIV["mixed"] * scale
 
 
-@pytest.mark.parametrize("mode", ["fast", "exact"])
-def test_w_sample_matches_oracle(mode, w, built_lib, oracle_lib):
+@pytest.mark.parametrize("mode,tree", [("fast", "kd"), ("exact", "kd"), ("fast", "morton")])
+def test_w_sample_matches_oracle(mode, tree, w, built_lib, oracle_lib):
     idx = w["idx"]
-    om, xo, L, sens = _sensitivity(w, {"evalMode": mode}, idx)
+    opts = {"evalMode": mode, "treeBuild": tree}
+    om, xo, L, sens = _sensitivity(w, opts, idx)
     so = om.stats()
     sub = dict(w)
     sub["xv0"] = w["xv0"][idx]
     for prec in ("fp64", "mixed"):
         bar = max(TOL[prec], 4 * sens)
         # the sampled nodes alone: errors and decision counts for those nodes
-        g = build_gpu(sub, {"evalMode": mode}, precision=prec)
+        g = build_gpu(sub, opts, precision=prec)
         g.setSurfaceCoordinates(w["xs"])
         g.warpMesh()
         err = np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / L
@@ -131,7 +137,7 @@ def test_w_sample_matches_oracle(mode, w, built_lib, oracle_lib):
         # of FP64 pairs otherwise), read at the sampled nodes
         if prec == "fp64" and mode == "exact":
             continue
-        g = build_gpu(w, {"evalMode": mode}, precision=prec)
+        g = build_gpu(w, opts, precision=prec)
         g.setSurfaceCoordinates(w["xs"])
         g.warpMesh()
         err = np.abs(g.getWarpGrid().reshape(-1, 3)[idx] - xo).max() / L
