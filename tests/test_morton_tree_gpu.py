@@ -27,7 +27,8 @@ MORTON = {"treeBuild": "morton"}
 def _mesh(name, planes=0):
     m = dict(sphere_small() if name == "sphere" else wing_small())
     if planes:
-        m["symmetryPlanes"] = [[[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]]]
+        m["symmetryPlanes"] = [[[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]], [[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]],
+                               [[0.0, 0.0, 0.0], [0.0, 1.0, 0.0]]][:planes]
     return m
 
 
@@ -183,3 +184,42 @@ def test_fast_error_report(name, built_lib):
             g.warpMesh()
             err[tb] = np.abs(g.getWarpGrid() - xe).max() / L
         assert err["morton"] <= ERR_FACTOR * err["kd"], (tol, err)
+
+
+@pytest.mark.parametrize("opts,planes", [
+    ({"aExp": 2.5, "bExp": 4.5}, 0),   # real-valued exponents: the third weight law
+    ({"aExp": 4.0, "bExp": 6.0}, 1),
+    ({"LdefFact": 100.0}, 0),
+    ({}, 3),
+])
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL_FP64), ("mixed", TOL_MIXED)])
+def test_laws_and_planes(opts, planes, precision, tol, built_lib, oracle_lib):
+    m = _mesh("sphere", planes)
+    o = dict(MORTON, **opts)
+    om = build_oracle(m, o)
+    g = build_gpu(m, o, precision=precision)
+    om.set_surface_coordinates(m["xs"])
+    g.setSurfaceCoordinates(m["xs"])
+    xo = om.warp()
+    g.warpMesh()
+    if precision == "mixed" and opts.get("aExp", 3.0) % 1.0:
+        tol = 1e-7  # real-valued exponents: FP32 powers throughout, as with the kd tree
+    assert np.abs(g.getWarpGrid().reshape(-1, 3) - xo).max() / om.ldef0() < tol
+    so, sg = om.stats(), g.getStats()
+    assert sg["leafPairs"] == so["leafPairs"] and sg["approx"] == so["approx"]
+
+
+def test_deterministic_reverse_product(built_lib):
+    # the deterministic mode on the Morton tree: bitwise repeatable, within
+    # the atomics' rounding of the default
+    m = _mesh("wing", 1)
+    dxv = np.random.default_rng(8).standard_normal(m["xv0"].shape)
+    out = []
+    for det in (True, True, False):
+        g = build_gpu(m, dict(MORTON, deterministic=det), precision="mixed")
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        g.warpDeriv(dxv.ravel(), solverVec=False)
+        out.append(g.getdXs().copy())
+    np.testing.assert_array_equal(out[0], out[1])
+    assert np.abs(out[0] - out[2]).max() <= 1e-12 * np.abs(out[2]).max()
