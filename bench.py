@@ -67,10 +67,10 @@ def mesh_options(m, precision, mode="fast", tree=None):
             "deterministic": DETERMINISTIC}
 
 
-def build_mesh(m, precision, mode="fast", restartFile=None):
+def build_mesh(m, precision, mode="fast", restartFile=None, tree=None):
     from idwarp_gb300 import USMesh
 
-    o = dict(mesh_options(m, precision, mode))
+    o = dict(mesh_options(m, precision, mode, tree))
     if restartFile:
         o["restartFile"] = restartFile
     with contextlib.redirect_stdout(io.StringIO()):
@@ -1112,6 +1112,45 @@ def main():
                               "setup_s_loaded": t_loaded, "loaded": mr.restartStatus,
                               "file_bytes": os.path.getsize(rf)}
             del mr
+        # the GPU-built Morton tree (option treeBuild "morton"; the reference
+        # builds the kd tree) on the same workload: set-up, the replayed warp,
+        # its work, and its fast-mode grid against the kd tree's
+        if TREE_BUILD == "kd":
+            t0 = time.perf_counter()
+            mm = build_mesh(m, "mixed", args.mode, tree="morton")
+            torch.cuda.synchronize()
+            t_m = time.perf_counter() - t0
+            Lm = mm.lib
+            Lm.idw_set_stream(mm.ctx, C.c_void_p(stream.cuda_stream))
+
+            def step_m():
+                _lib.check(Lm, mm.ctx, Lm.idw_set_surface_coordinates(mm.ctx, xs_ptr, 3 * npts, _lib.IDW_DEVICE),
+                           "setSurfaceCoordinates")
+                _lib.check(Lm, mm.ctx, Lm.idw_warp_mesh(mm.ctx), "warpMesh")
+
+            t0 = time.perf_counter()
+            step_m()
+            torch.cuda.synchronize()
+            first_m = time.perf_counter() - t0
+            step_m()
+            m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            m0.record(stream)
+            for _ in range(5):
+                step_m()
+            m1.record(stream)
+            torch.cuda.synchronize()
+            ms_m = m0.elapsed_time(m1) / 5
+            stm = mm.getStats()
+            dk = np.abs(mm.getWarpGrid().reshape(-1, 3) - grid.reshape(-1, 3)).max(axis=1) / Ldef
+            out["morton_tree"] = {"setup_s": t_m, "setup_s_kd": setup_s, "tree_build_ms": stm["treeBuildMs"],
+                                  "tree_build_ms_kd": st["treeBuildMs"], "first_warp_s": first_m,
+                                  "ms_per_step": ms_m, "value": nvol / (ms_m * 1e-3), "unit": "volume nodes/s",
+                                  "leafPairs": stm["leafPairs"], "approx": stm["approx"],
+                                  "max_diff_vs_kd_over_Ldef": float(dk.max()),
+                                  "rms_diff_vs_kd_over_Ldef": float(np.sqrt(np.mean(dk ** 2))),
+                                  "note": "other clusters than the reference's kd tree: fast-mode grids differ by "
+                                          "what errTol allows (error against exact mode: bench.py --suite-tree)"}
+            del mm
 
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"], idx, xv_cpu = run_cpu_baseline(m)
