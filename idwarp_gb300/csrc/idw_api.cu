@@ -544,6 +544,7 @@ int idw_initialize_warping(void *ctx, const double *pts, int32_t npts, const dou
     if (c->opt.treeBuild == IDW_TREE_MORTON) {
         const int rc = build_morton_tree(uniquepts, nunique, c->opt.bucketSize, t, c->stream);
         if (rc == -2) return fail(c, IDW_ERR_NOMEM, "out of device memory in the surface tree build");
+        if (rc == -3) return fail(c, IDW_ERR_LIMIT, "the Morton tree takes at most 2^30 unique surface points");
         if (rc != 0) return fail(c, IDW_ERR_CUDA, "surface tree build: %s", cudaGetErrorString(cudaGetLastError()));
     } else {
         build_kdtree(uniquepts, nunique, c->opt.bucketSize, t);

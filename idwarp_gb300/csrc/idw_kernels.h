@@ -290,7 +290,8 @@ void launch_nodal_b_faces(const SurfaceDev &s, const double *Xu, int useRotation
 
 // Surface tree built on the device (idw_tree.cu): Morton order, binary radix
 // tree cut at bucket-size leaves, in the host kd build's layout.  pts: host
-// array of n unique points.  0, -1 (CUDA error) or -2 (out of device memory).
+// array of n unique points.  0, -1 (CUDA error), -2 (out of device memory) or
+// -3 (more than 2^30 points).
 struct FlatTree;
 int build_morton_tree(const double *pts, int n, int bucket, FlatTree &t, cudaStream_t st);
 

@@ -315,7 +315,7 @@ int build_morton_tree(const double *pts, int n, int bucket, FlatTree &t, cudaStr
     t.n = n;
     t.bucket = bucket;
     if (n <= 0) return 0;
-    if (n > (INT_MAX - 1) / 2) return -1;
+    if (n > (INT_MAX - 1) / 2) return -3;  // radix node ids are int
     const int nr = 2 * n - 1;  // radix nodes; at most nr are kept
     // cub scratch: the larger of the two sorts and the scan
     size_t tmpA = 0, tmpB = 0, tmpC = 0;
