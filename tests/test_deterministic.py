@@ -129,3 +129,48 @@ def test_capture_refused(built_lib):
         torch.zeros(1, device="cuda")  # the graph holds one node of its own
     assert rc == _lib.IDW_ERR_STATE
     torch.cuda.synchronize()
+
+
+def test_concurrent_contexts(built_lib):
+    # two host threads with their own contexts: deterministic reverse products
+    # in one (serialised in the process, state in constant memory) and the
+    # default ones in the other (their kernels never read that state)
+    import ctypes as C
+    import threading
+
+    import torch
+
+    m = wing_small()
+    dxv = np.random.default_rng(7).standard_normal(m["xv0"].shape).ravel()
+    gd = build_gpu(m, {"deterministic": True}, precision="mixed")
+    ga = build_gpu(m, precision="mixed")
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]  # kernels of the two contexts may overlap
+    for g, st in zip((gd, ga), streams):
+        g.lib.idw_set_stream(g.ctx, C.c_void_p(st.cuda_stream))
+    refs = {}
+    for name, g in (("det", gd), ("atomic", ga)):
+        g.setSurfaceCoordinates(m["xs"])
+        g.warpMesh()
+        g.warpDeriv(dxv, solverVec=False)
+        refs[name] = g.getdXs().copy()
+    errors = []
+
+    def run(name, g, n):
+        try:
+            for _ in range(n):
+                g.warpDeriv(dxv, solverVec=False)
+                out = g.getdXs()
+                if name == "det":
+                    if not np.array_equal(out, refs[name]):
+                        errors.append((name, "not bitwise"))
+                elif np.abs(out - refs[name]).max() > 1e-12 * np.abs(refs[name]).max():
+                    errors.append((name, float(np.abs(out - refs[name]).max())))
+        except Exception as e:  # the thread's failure is the test's
+            errors.append((name, repr(e)))
+
+    threads = [threading.Thread(target=run, args=("det", gd, 4)), threading.Thread(target=run, args=("atomic", ga, 8))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
