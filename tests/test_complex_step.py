@@ -42,10 +42,12 @@ def s1():
     return m
 
 
-@pytest.mark.parametrize("case,mode", [("s1", "fast"), ("wing", "fast"), ("wing", "exact")])
-def test_complex_step_matches_derivatives(case, mode, s1, built_lib, oracle_lib):
+@pytest.mark.parametrize("case,mode,tree", [("s1", "fast", "kd"), ("wing", "fast", "kd"), ("wing", "exact", "kd"),
+                                             ("wing", "fast", "morton")])
+def test_complex_step_matches_derivatives(case, mode, tree, s1, built_lib, oracle_lib):
+    # tree "morton": the same checks on the GPU-built tree (the oracle builds it too)
     m = s1 if case == "s1" else wing_small()
-    opts = {"evalMode": mode}
+    opts = {"evalMode": mode, "treeBuild": tree}
     gc = _usmesh_c(m, opts)
     coords0 = gc.getSurfaceCoordinates()
     assert coords0.dtype == np.complex128
