@@ -28,21 +28,47 @@ namespace idw {
 
 namespace {
 
+// Shared-memory targets of a batch of cluster terms (batches of more than two
+// terms); for two, the kernel keeps them in registers: 16 seeds fill shared
+// memory to exactly four blocks per SM, and 8 more bytes per warp make it three.
+template <bool SMEM, int KP>
+struct PrecTargets {
+    int tgt[KP];  // tree nodes of a batch of cluster terms
+};
+template <int KP>
+struct PrecTargets<false, KP> {};
+
+#ifndef IDW_PREC_KP16
+#define IDW_PREC_KP16 2
+#endif
+
 template <int S>
-struct PrecSmem {
+struct PrecSmem : PrecTargets<(S > 0 && (S <= 4 ? 10 : IDW_PREC_KP16) > 2), (S <= 4 ? 10 : IDW_PREC_KP16)> {
     static constexpr int kC = S > 0 ? 3 * S : 1;
     // leaf points reduced per shared-memory pass: a whole leaf of the default
     // bucket (up to 9 points) in one pass for few seeds; 2 for 16 seeds, whose
     // seed arrays fill shared memory (per warp 20 KB with 8 points: two blocks
     // per SM; 16 KB with 4: three; 14 KB with 2: four; 726, 586 and 527 ms at
     // 8M nodes)
-#ifndef IDW_PREC_KP16
-#define IDW_PREC_KP16 2
-#endif
     static constexpr int kP = S == 0 ? 1 : (S <= 4 ? 10 : IDW_PREC_KP16);
     float nh[32][kC], nl[32][kC];      // seeds of every lane (numb, scaled), hi / lo
     float4 vh[kP][32], vl[kP][32];     // per term: w, w (r - C), hi / lo
 };
+
+template <int S>
+__host__ __device__ constexpr bool prec_smem_targets() {
+    return S > 0 && PrecSmem<S>::kP > 2;
+}
+// 16 seeds at two points per pass: 14 KB per warp, four blocks per SM
+static_assert(IDW_PREC_KP16 != 2 || sizeof(PrecSmem<16>) == 2 * 32 * 48 * 4 + 2 * 2 * 32 * 16,
+              "the 16-seed shared-memory layout sets the occupancy");
+
+// Cluster terms wait in vh / vl until kP of them (or a leaf, or the end of the
+// mirror pass) and are reduced together, one task per (term, seed component)
+// as leaf points are, instead of one warp reduction per term.
+#ifndef IDW_PREC_CBATCH
+#define IDW_PREC_CBATCH 1
+#endif
 
 // acc += a * b in double-float (error-free product, then two-sum).
 __device__ __forceinline__ void df_fma_acc(dfl &acc, dfl a, dfl b) {
@@ -63,8 +89,11 @@ __device__ __forceinline__ void land_df(double *d, dfl v) {
 // Reduction of m terms (vh/vl[0..m)) against the lanes' seeds: one (term,
 // seed component) pair per lane task, each summing the 32 lanes in
 // double-float; lands w -> slot 9 + a and w (r - C) -> slots 3 a .. 3 a + 2.
+// batch: the terms are a batch of cluster terms, targets in sm.tgt (or bt0,
+// bt1 for batches of at most two); otherwise points base .. base + m - 1.
 template <int S, bool DET>
-__device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
+__device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base, double *adj, int64_t seedStride,
+                                                bool batch = false, int bt0 = 0, int bt1 = 0) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     for (int task = lane; task < 3 * S * m; task += 32) {
@@ -80,7 +109,12 @@ __device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base
             df_fma_acc(a3, {vh.w, vl.w}, n);
         }
         const int s = c / 3, a = c - 3 * s;
-        double *d = adj + s * seedStride + 12 * int64_t(base + p);
+        int tg = base + p;
+        if (batch) {
+            if constexpr (prec_smem_targets<S>()) tg = sm.tgt[p];
+            else tg = p == 0 ? bt0 : bt1;
+        }
+        double *d = adj + s * seedStride + 12 * int64_t(tg);
         land_df<DET>(d + 9 + a, a0);
         land_df<DET>(d + 3 * a + 0, a1);
         land_df<DET>(d + 3 * a + 1, a2);
@@ -181,6 +215,14 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
     MixedCounters cnt;
     float dsum = 0.f, dcomp = 0.f;  // S = 0: this lane's denominator (all mirrors)
     dfl nl1[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};  // S = 1: this lane's seed
+    int npend = 0, pt0 = 0, pt1 = 0;  // cluster terms waiting in sm.vh / vl (warp-uniform)
+    auto flush = [&]() {
+        if (npend) {
+            reduce_tasks_df<(S > 0 ? S : 1), DET>(reinterpret_cast<PrecSmem<(S > 0 ? S : 1)> &>(sm), npend, 0,
+                                                  nodeAdj, nodeStride, true, pt0, pt1);
+            npend = 0;
+        }
+    };
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
         const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
@@ -228,6 +270,7 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
             }
             const int4 inf = ldgi4(&tf.nodes[node].info);
             if (inf.w) {
+                if constexpr (S > 0 && IDW_PREC_CBATCH) flush();  // the leaf reuses vh / vl
                 const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                 dfl R[3];
                 rel_df(rh, rl, ch, cl, R);
@@ -296,7 +339,17 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                     } else {
                         dfl vv[4];
                         term_vector(wh, wl, x, vv);
-                        if constexpr (S == 1) {
+                        if constexpr (IDW_PREC_CBATCH) {
+                            sm.vh[npend][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
+                            sm.vl[npend][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
+                            if constexpr (prec_smem_targets<S>()) {
+                                if (lane == 0) sm.tgt[npend] = node;
+                            } else {
+                                if (npend == 0) pt0 = node;
+                                else pt1 = node;
+                            }
+                            if (++npend == PrecSmem<S>::kP) flush();
+                        } else if constexpr (S == 1) {
                             land_one_df<DET>(vv, nl1, nodeAdj + 12 * int64_t(node));
                         } else {
                             sm.vh[0][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
@@ -311,6 +364,7 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                 }
             }
         }
+        if constexpr (S > 0 && IDW_PREC_CBATCH) flush();  // before the next pass's seeds
         __syncwarp();
     }
     if (S == 0 && valid) denOut[vi] = (double(dsum) + double(dcomp)) * exp2(-double(s) * mp.bExp);
