@@ -63,11 +63,13 @@ __host__ __device__ constexpr bool prec_smem_targets() {
 static_assert(IDW_PREC_KP16 != 2 || sizeof(PrecSmem<16>) == 2 * 32 * 48 * 4 + 2 * 2 * 32 * 16,
               "the 16-seed shared-memory layout sets the occupancy");
 
-// Cluster terms wait in vh / vl until kP of them (or a leaf, or the end of the
-// mirror pass) and are reduced together, one task per (term, seed component)
-// as leaf points are, instead of one warp reduction per term.
+// Terms wait in vh / vl until kP of them (or the end of the mirror pass) and
+// are reduced together, one task per (term, seed component), instead of one
+// reduction per cluster term and per leaf (whose few points leave task lanes
+// idle).  IDW_PREC_CBATCH: 0 none, 1 cluster terms (flushed at each leaf), 2
+// every term.
 #ifndef IDW_PREC_CBATCH
-#define IDW_PREC_CBATCH 1
+#define IDW_PREC_CBATCH 2
 #endif
 
 // acc += a * b in double-float (error-free product, then two-sum).
@@ -89,11 +91,13 @@ __device__ __forceinline__ void land_df(double *d, dfl v) {
 // Reduction of m terms (vh/vl[0..m)) against the lanes' seeds: one (term,
 // seed component) pair per lane task, each summing the 32 lanes in
 // double-float; lands w -> slot 9 + a and w (r - C) -> slots 3 a .. 3 a + 2.
-// batch: the terms are a batch of cluster terms, targets in sm.tgt (or bt0,
-// bt1 for batches of at most two); otherwise points base .. base + m - 1.
+// batch: the terms are a batch, targets in sm.tgt (or bt0, bt1 for batches of
+// at most two): a point index, or ~node for a cluster term (landed in nodeAdj);
+// otherwise points base .. base + m - 1.
 template <int S, bool DET>
 __device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base, double *adj, int64_t seedStride,
-                                                bool batch = false, int bt0 = 0, int bt1 = 0) {
+                                                bool batch = false, int bt0 = 0, int bt1 = 0,
+                                                double *nodeAdj = nullptr, int64_t nodeStride = 0) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     for (int task = lane; task < 3 * S * m; task += 32) {
@@ -114,7 +118,7 @@ __device__ __forceinline__ void reduce_tasks_df(PrecSmem<S> &sm, int m, int base
             if constexpr (prec_smem_targets<S>()) tg = sm.tgt[p];
             else tg = p == 0 ? bt0 : bt1;
         }
-        double *d = adj + s * seedStride + 12 * int64_t(tg);
+        double *d = tg >= 0 ? adj + s * seedStride + 12 * int64_t(tg) : nodeAdj + s * nodeStride + 12 * int64_t(~tg);
         land_df<DET>(d + 9 + a, a0);
         land_df<DET>(d + 3 * a + 0, a1);
         land_df<DET>(d + 3 * a + 1, a2);
@@ -215,13 +219,27 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
     MixedCounters cnt;
     float dsum = 0.f, dcomp = 0.f;  // S = 0: this lane's denominator (all mirrors)
     dfl nl1[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};  // S = 1: this lane's seed
-    int npend = 0, pt0 = 0, pt1 = 0;  // cluster terms waiting in sm.vh / vl (warp-uniform)
+    int npend = 0, pt0 = 0, pt1 = 0;  // terms waiting in sm.vh / vl (warp-uniform)
     auto flush = [&]() {
         if (npend) {
             reduce_tasks_df<(S > 0 ? S : 1), DET>(reinterpret_cast<PrecSmem<(S > 0 ? S : 1)> &>(sm), npend, 0,
-                                                  nodeAdj, nodeStride, true, pt0, pt1);
+                                                  ptAdj, ptStride, true, pt0, pt1, nodeAdj, nodeStride);
             npend = 0;
         }
+    };
+    // one term into the batch: target = point index, or ~node for a cluster
+    auto push = [&](const dfl *vv, int target) {
+        constexpr int SS = S > 0 ? S : 1;
+        auto &smb = reinterpret_cast<PrecSmem<SS> &>(sm);
+        smb.vh[npend][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
+        smb.vl[npend][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
+        if constexpr (prec_smem_targets<SS>()) {
+            if (lane == 0) smb.tgt[npend] = target;
+        } else {
+            if (npend == 0) pt0 = target;
+            else pt1 = target;
+        }
+        if (++npend == PrecSmem<SS>::kP) flush();
     };
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
@@ -270,7 +288,7 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
             }
             const int4 inf = ldgi4(&tf.nodes[node].info);
             if (inf.w) {
-                if constexpr (S > 0 && IDW_PREC_CBATCH) flush();  // the leaf reuses vh / vl
+                if constexpr (S > 0 && IDW_PREC_CBATCH == 1) flush();  // the leaf reuses vh / vl
                 const float4 ch = ldgf4(&tf.nodes[node].cHi), cl = ldgf4(&tf.nodes[node].cLo);
                 dfl R[3];
                 rel_df(rh, rl, ch, cl, R);
@@ -278,14 +296,12 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                     cnt.leafPairs += inf.y - inf.x + 1;
                     cnt.visited++;
                 }
-                for (int i0 = inf.x; i0 <= inf.y; i0 += PrecSmem<S>::kP) {
-                    const int m = min(PrecSmem<S>::kP, inf.y - i0 + 1);
-                    for (int p = 0; p < m; ++p) {
-                        const int i = i0 + p;
+                if constexpr (S > 0 && IDW_PREC_CBATCH >= 2) {
+                    // every point into the batch
+                    for (int i = inf.x; i <= inf.y; ++i) {
                         float wh = 0.f, wl = 0.f;
                         dfl xr[3];
                         if (active) {
-                            // r - Xu0_i = (r - C) - (Xu0_i - C), offsets from the leaf centroid
                             const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
                             dfl x[3];
                             two_diff(R[0].h, da.x, x[0].h, x[0].l);
@@ -296,17 +312,41 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                             x[2].l += R[2].l - dl.z;
                             precise_weight<KIND>(x, 1e-15f, da.w, dl.w, law, Ls, LsLo, c1, mp.abH, mp.abL, xr, wh, wl);
                         }
-                        if constexpr (S == 0) {
-                            comp_add_df(dsum, dcomp, wh, wl);
-                        } else {
-                            // moments relative to the leaf centroid
-                            dfl vv[4];
-                            term_vector(wh, wl, R, vv);
-                            sm.vh[p][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
-                            sm.vl[p][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
-                        }
+                        dfl vv[4];
+                        term_vector(wh, wl, R, vv);  // moments relative to the leaf centroid
+                        push(vv, i);
                     }
-                    if constexpr (S > 0) reduce_tasks_df<S, DET>(sm, m, i0, ptAdj, ptStride);
+                } else {
+                    for (int i0 = inf.x; i0 <= inf.y; i0 += PrecSmem<S>::kP) {
+                        const int m = min(PrecSmem<S>::kP, inf.y - i0 + 1);
+                        for (int p = 0; p < m; ++p) {
+                            const int i = i0 + p;
+                            float wh = 0.f, wl = 0.f;
+                            dfl xr[3];
+                            if (active) {
+                                // r - Xu0_i = (r - C) - (Xu0_i - C), offsets from the leaf centroid
+                                const float4 da = ldgf4(pf.da + i), dl = ldgf4(pf.dl + i);
+                                dfl x[3];
+                                two_diff(R[0].h, da.x, x[0].h, x[0].l);
+                                two_diff(R[1].h, da.y, x[1].h, x[1].l);
+                                two_diff(R[2].h, da.z, x[2].h, x[2].l);
+                                x[0].l += R[0].l - dl.x;
+                                x[1].l += R[1].l - dl.y;
+                                x[2].l += R[2].l - dl.z;
+                                precise_weight<KIND>(x, 1e-15f, da.w, dl.w, law, Ls, LsLo, c1, mp.abH, mp.abL, xr, wh, wl);
+                            }
+                            if constexpr (S == 0) {
+                                comp_add_df(dsum, dcomp, wh, wl);
+                            } else {
+                                // moments relative to the leaf centroid
+                                dfl vv[4];
+                                term_vector(wh, wl, R, vv);
+                                sm.vh[p][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
+                                sm.vl[p][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
+                            }
+                        }
+                        if constexpr (S > 0) reduce_tasks_df<S, DET>(sm, m, i0, ptAdj, ptStride);
+                    }
                 }
                 if (!REPLAY) node = inf.z;
             } else {
@@ -340,15 +380,7 @@ __global__ void __launch_bounds__(128) k_adjoint_precise(TreeDev t, TreeDevF tf,
                         dfl vv[4];
                         term_vector(wh, wl, x, vv);
                         if constexpr (IDW_PREC_CBATCH) {
-                            sm.vh[npend][lane] = make_float4(vv[0].h, vv[1].h, vv[2].h, vv[3].h);
-                            sm.vl[npend][lane] = make_float4(vv[0].l, vv[1].l, vv[2].l, vv[3].l);
-                            if constexpr (prec_smem_targets<S>()) {
-                                if (lane == 0) sm.tgt[npend] = node;
-                            } else {
-                                if (npend == 0) pt0 = node;
-                                else pt1 = node;
-                            }
-                            if (++npend == PrecSmem<S>::kP) flush();
+                            push(vv, ~node);
                         } else if constexpr (S == 1) {
                             land_one_df<DET>(vv, nl1, nodeAdj + 12 * int64_t(node));
                         } else {
