@@ -31,7 +31,17 @@ struct AdjSmem {
     // groups reading different points hit different banks
     static constexpr int kRow = S == 8 ? 33 : 32;
     float4 vb[kChunk][kRow];
+    int tgt[S <= 4 ? kChunk : 1];  // few seeds: targets of a batch of terms
 };
+
+// Few seeds (S <= 4): a warp's terms, leaf points and approximated clusters
+// alike, wait in vb until kChunk of them (or the end of the mirror pass) and
+// reduce together, one lane task per (term, seed component), instead of one
+// reduction per leaf (about 5.5 points: half the task lanes idle) and one
+// warp butterfly per cluster term.
+#ifndef IDW_ADJ_BATCH
+#define IDW_ADJ_BATCH 1
+#endif
 
 // Lands the four moment sums of term `target`, seed component c (seed s, axis
 // a): w -> B (slot 9 + a), w (r - C) -> row a of P (slots 3a .. 3a + 2).
@@ -133,8 +143,11 @@ __device__ __forceinline__ void reduce_groups(AdjSmem<S> &sm, int m, int base, d
 // task, so that 3 S m tasks keep the warp busy where 3 S lanes alone would
 // not.  Each task walks the lanes starting at its term index, which spreads
 // the tasks of different terms over the shared-memory banks.
+// batch: targets in sm.tgt, a point index or ~node for a cluster term (landed
+// in nodeAdj); otherwise points base .. base + m - 1.
 template <int S, bool DET>
-__device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride) {
+__device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, double *adj, int64_t seedStride,
+                                             bool batch = false, double *nodeAdj = nullptr, int64_t nodeStride = 0) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     for (int task = lane; task < 3 * S * m; task += 32) {
@@ -150,7 +163,13 @@ __device__ __forceinline__ void reduce_tasks(AdjSmem<S> &sm, int m, int base, do
             a2 = fmaf(v.z, nbv, a2);
             a3 = fmaf(v.w, nbv, a3);
         }
-        land_moments<DET>(adj, seedStride, c, base + p, a0, a1, a2, a3);
+        if (batch) {
+            const int tg = sm.tgt[p];
+            if (tg >= 0) land_moments<DET>(adj, seedStride, c, tg, a0, a1, a2, a3);
+            else land_moments<DET>(nodeAdj, nodeStride, c, ~tg, a0, a1, a2, a3);
+        } else {
+            land_moments<DET>(adj, seedStride, c, base + p, a0, a1, a2, a3);
+        }
     }
     __syncwarp();
 }
@@ -201,6 +220,20 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
     // measured 6% faster at 8M nodes (161.5 vs 171.9 ms)
     int targets[S >= 8 ? kChunk : 1];
     float nl[3] = {0.f, 0.f, 0.f};  // one seed: this lane's, kept in registers
+    constexpr bool kBatch = IDW_ADJ_BATCH && S <= 4;
+    int npend = 0;  // few seeds: terms waiting in sm.vb (warp-uniform)
+    auto flush = [&]() {
+        if (npend) {
+            reduce_tasks<S, DET>(sm, npend, 0, ptAdj, ptStride, true, nodeAdj, nodeStride);
+            npend = 0;
+        }
+    };
+    // one term into the batch: target = point index, or ~node for a cluster
+    auto push = [&](const float4 vv, int target) {
+        sm.vb[npend][lane] = vv;
+        if (lane == 0) sm.tgt[npend] = target;
+        if (++npend == kChunk) flush();
+    };
     for (int kk = 0; kk < mp.nLoop; ++kk) {
         const float4 rhi = rec.hi[kk * v.nVol + g], rlo = rec.lo[kk * v.nVol + g];
         const float rh[3] = {rhi.x, rhi.y, rhi.z}, rl[3] = {rlo.x, rlo.y, rlo.z};
@@ -261,7 +294,18 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         cnt.visited++;
                     }
                     const float R0 = h0 + l0, R1 = h1 + l1, R2 = h2 + l2;
-                    for (int i0 = inf.x; i0 <= inf.y; i0 += kChunk) {
+                    if constexpr (kBatch) {
+                        for (int i = inf.x; i <= inf.y; ++i) {
+                            float w = 0.f;
+                            if (active) {
+                                float dx, dy, dz;
+                                w = leaf_weight<KIND>(law, Ls, LsLo, c1, ab, abl, h0, h1, h2, l0, l1, l2,
+                                                      ldgf4(pf.da + i), ldgf4(pf.dl + i), dx, dy, dz);
+                            }
+                            push(make_float4(w, w * R0, w * R1, w * R2), i);
+                        }
+                    }
+                    for (int i0 = inf.x; !kBatch && i0 <= inf.y; i0 += kChunk) {
                         const int m = min(kChunk, inf.y - i0 + 1);
                         for (int p = 0; p < m; ++p) {
                             const int i = i0 + p;
@@ -308,7 +352,9 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                         cnt.approx++;
                     }
                     const float4 vv = make_float4(w, w * rho0, w * rho1, w * rho2);
-                    if constexpr (S == 1) {
+                    if constexpr (kBatch) {
+                        push(vv, ~node);
+                    } else if constexpr (S == 1) {
                         reduce_one_s1<DET>(vv, nl, nodeAdj + 12 * int64_t(node));
                     } else {
                         sm.vb[0][lane] = vv;
@@ -326,6 +372,7 @@ __global__ void __launch_bounds__(128) k_adjoint_mixed(TreeDev t, TreeDevF tf, P
                 }
             }
         }
+        if constexpr (kBatch) flush();  // before the next pass's seeds
         __syncwarp();
     }
     if (!REPLAY) cnt.flush(counters);
