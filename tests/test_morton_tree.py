@@ -120,3 +120,122 @@ def test_struct_sizes_match_header(tmp_path):
     assert got == [C.sizeof(_lib.idw_options), C.sizeof(_lib.idw_stats), C.sizeof(_lib.idw_tuning),
                    _lib.idw_options.treeBuild.offset, _lib.idw_stats.treeBuildMs.offset,
                    _lib.idw_options.deterministic.offset]
+
+
+def _parallel_build(pts, bucket):
+    """The device build's index arithmetic (idw_tree.cu: k_tree_radix,
+    k_tree_keep, k_tree_nodes), one interior node at a time: direction and
+    range from the common-prefix lengths with the neighbours, the split by
+    binary search, the cut at bucket-size nodes, preorder by sorting the kept
+    ranges on (first ascending, last descending), escapes by binary search."""
+    import bisect
+
+    n = len(pts)
+    code = [int(c) for c in _codes(pts)]
+    perm = sorted(range(n), key=lambda i: code[i])  # stable: ties keep the point order
+    k = [code[i] for i in perm]
+
+    def prefix(i, j):
+        if j < 0 or j >= n:
+            return -1
+        if k[i] != k[j]:
+            return 64 - (k[i] ^ k[j]).bit_length()
+        return 64 + 32 - (i ^ j).bit_length()
+
+    nr = 2 * n - 1
+    parent = [-1] * nr
+    rng = [None] * max(n - 1, 1)
+    for i in range(n - 1):
+        d = 1 if prefix(i, i + 1) > prefix(i, i - 1) else -1
+        dmin = prefix(i, i - d)
+        lmax = 2
+        while prefix(i, i + lmax * d) > dmin:
+            lmax *= 2
+        ln, t = 0, lmax // 2
+        while t >= 1:
+            if prefix(i, i + (ln + t) * d) > dmin:
+                ln += t
+            t //= 2
+        j = i + ln * d
+        dnode = prefix(i, j)
+        s, div = 0, 2
+        while True:
+            t = (ln + div - 1) // div
+            if prefix(i, i + (s + t) * d) > dnode:
+                s += t
+            if t <= 1:
+                break
+            div *= 2
+        gamma = i + s * d + (-1 if d < 0 else 0)
+        lo, hi = min(i, j), max(i, j)
+        left = n - 1 + gamma if lo == gamma else gamma
+        right = n - 1 + gamma + 1 if hi == gamma + 1 else gamma + 1
+        rng[i] = (lo, hi)
+        assert parent[left] == -1 and parent[right] == -1  # every node has one parent
+        parent[left] = parent[right] = i
+    keys = []
+    for r in range(nr):
+        g = rng[r] if r < n - 1 else (r - (n - 1), r - (n - 1))
+        p = parent[r]
+        if p < 0 or rng[p][1] - rng[p][0] > bucket:
+            keys.append((g[0] << 32) | (0xFFFFFFFF - g[1]))
+    keys.sort()
+    nodes = []
+    for kk, key in enumerate(keys):
+        lo, hi = key >> 32, 0xFFFFFFFF - (key & 0xFFFFFFFF)
+        esc = bisect.bisect_left(keys, (hi + 1) << 32, kk + 1)
+        nodes.append((lo, hi, esc, hi - lo <= bucket))
+    return perm, nodes
+
+
+@pytest.mark.parametrize("bucket", [1, 8])
+@pytest.mark.parametrize("name", ["sphere", "wing"])
+def test_parallel_construction_equals_oracle(name, bucket, oracle_lib):
+    from oracle.pyoracle import point_reduce
+
+    m = _mesh(name)
+    om = build_oracle(m, {"treeBuild": "morton", "bucketSize": bucket})
+    t = om.tree()
+    uniq, _, _ = point_reduce(m["pts"])
+    srt = uniq[np.lexsort(uniq.T)]  # the unique points in the order the tree receives them
+    perm, nodes = _parallel_build(srt, bucket)
+    np.testing.assert_array_equal(srt[perm], om.surface()["Xu0"])
+    nodes = np.array(nodes)
+    np.testing.assert_array_equal(nodes[:, 0], t["l"])
+    np.testing.assert_array_equal(nodes[:, 1], t["u"])
+    np.testing.assert_array_equal(nodes[:, 2], t["escape"])
+    np.testing.assert_array_equal(nodes[:, 3] == 1, t["dnum"] == 0)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 9, 100, 700])
+def test_parallel_construction_random_clouds(n):
+    # tied codes (points 1e-12 apart) and tiny clouds; the radius pass's
+    # 256-point tasks (k_tree_radius) cover every (node, point) pair once
+    rng = np.random.default_rng(n)
+    pts = rng.standard_normal((n, 3))
+    if n > 10:
+        pts[n // 2:n // 2 + 5] = pts[n // 2] + 1e-12 * np.arange(5)[:, None]
+    for bucket in (1, 2, 8):
+        _, nodes = _parallel_build(pts, bucket)
+        nodes = np.array(nodes)
+        leaf = nodes[:, 3] == 1
+        lv = nodes[leaf]
+        assert lv[0, 0] == 0 and lv[-1, 1] == n - 1 and np.all(lv[1:, 0] == lv[:-1, 1] + 1)
+        for kk in np.flatnonzero(~leaf):
+            a = kk + 1
+            b = nodes[a, 2]
+            assert nodes[a, 0] == nodes[kk, 0] and nodes[b, 1] == nodes[kk, 1] and nodes[b, 0] == nodes[a, 1] + 1
+        for task in (256, 4):
+            chunks = (nodes[:, 1] - nodes[:, 0] + task) // task
+            incl = np.cumsum(chunks)
+            seen = set()
+            for c in range(int(incl[-1])):
+                a = int(np.searchsorted(incl, c, side="right"))
+                first = incl[a] - chunks[a]
+                i0 = nodes[a, 0] + (c - first) * task
+                i1 = min(nodes[a, 1], i0 + task - 1)
+                assert nodes[a, 0] <= i0 <= i1 <= nodes[a, 1]
+                for i in range(i0, i1 + 1):
+                    assert (a, i) not in seen
+                    seen.add((a, i))
+            assert len(seen) == int((nodes[:, 1] - nodes[:, 0] + 1).sum())
